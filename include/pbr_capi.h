@@ -1,0 +1,152 @@
+/*
+ * pbr_capi.h -- C ABI of libpbr.so, the GB300 (sm_103a) batch renderer.
+ *
+ * The reference renders through Panda3D + OpenGL: per-instance matrices and
+ * colours live in buffer textures uploaded with Texture.set_ram_image
+ * (renderer/node.py:85-91,110-114,156-161), per-scene view-projection matrices
+ * and tile rectangles in two more buffer textures (renderer/camera.py:29-30,
+ * 110-135,146-148), lighting in shader uniforms (renderer/light.py:26-44),
+ * one instanced draw per node runs shaders/basic.{vert,frag}, and the atlas is
+ * read back and rearranged into [N,C,H,W] (renderer/renderer.py:326-363,
+ * renderer/frame_grabber.py:85-106).  This ABI replaces that whole layer:
+ * the caller keeps the scene state in device buffers it owns, binds their
+ * addresses once, and every render call writes the final [N,C,H,W] pixels
+ * directly into a caller-owned device tensor.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: PBR_OK (0) or a PBR_ERR_* code.
+ *    pbr_last_error() returns a message for the last failing call on a context
+ *    (or, with ctx == NULL, for the last failing pbr_create on this thread).
+ *  - Pointers named d_* are device pointers on the context's device.  They are
+ *    borrowed, never freed: the caller keeps them alive while they are bound.
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default
+ *    stream.  Render/backward calls only enqueue kernels and asynchronous
+ *    memsets on that stream: no host synchronisation and no allocation, so
+ *    they may be captured into a CUDA graph.  Binding calls change kernel
+ *    arguments; a graph captured before a rebind keeps the old arguments.
+ *  - One context belongs to one host thread at a time.
+ */
+#ifndef PBR_CAPI_H
+#define PBR_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pbr_ctx pbr_ctx;
+
+#define PBR_OK 0
+#define PBR_ERR_INVALID 1   /* bad argument (shape, pointer, range) */
+#define PBR_ERR_CUDA 2      /* a CUDA runtime call failed */
+#define PBR_ERR_CAPACITY 3  /* a fixed table or id range is exceeded */
+#define PBR_ERR_STATE 4     /* call order (e.g. render before a camera is bound) */
+#define PBR_ERR_DEVICE 5    /* a kernel reported an error flag (see pbr_device_status) */
+
+/* Instance rotation encodings for pbr_node_set_buffers(mode). */
+#define PBR_MODE_HPR 0  /* d_rot = [B,3] heading/pitch/roll in radians, R = Rz(H) Ry(P) Rx(R) */
+#define PBR_MODE_ROT 1  /* d_rot = [B,9] row-major 3x3 rotation */
+#define PBR_MODE_MAT 2  /* d_rot = [B,16] row-major 4x4 model matrix; d_pos, d_scale unused */
+
+/* Library version (major*10000 + minor*100 + patch).  No counterpart in the
+ * reference. */
+int pbr_version(void);
+
+/* Message for the last failing call.  Never NULL. */
+const char* pbr_last_error(const pbr_ctx* ctx);
+
+/* Create a renderer for num_scenes scenes of width x height pixels with
+ * `channels` output channels (1..4: R, G, B, A).  Replaces the window/atlas
+ * set-up of PBRRenderer.__init__ + _setup_offscreen_rt
+ * (renderer/renderer.py:39-89,253-287) and PBRConfig.process_resolution
+ * (config.py:61-126): scenes are a flat batch, there is no atlas.
+ * flags: reserved, pass 0. */
+int pbr_create(pbr_ctx** out_ctx, int num_scenes, int width, int height, int channels, int flags);
+int pbr_destroy(pbr_ctx* ctx);
+
+/* Register a triangle mesh already resident on the device: d_pos [nv,3],
+ * d_nrm [nv,3] (unit normals), d_idx [nt,3] counter-clockwise seen from
+ * outside.  smooth = 0 when every triangle's three normals are equal (flat
+ * shading is then resolved once per triangle).  Replaces the model load +
+ * flattenStrong of PBRNode.__init__ (renderer/node.py:61-71). */
+int pbr_mesh_register(pbr_ctx* ctx, const float* d_pos, const float* d_nrm, const int32_t* d_idx,
+                      int nv, int nt, int smooth, int* out_mesh_id);
+
+/* Add a node: one mesh drawn instances_per_scene times in every scene.
+ * shared != 0 means instance i of every scene reads buffer row i
+ * (B = instances_per_scene rows), otherwise scene k instance i reads row
+ * k*instances_per_scene + i (B = N*instances_per_scene rows).  Replaces
+ * PBRNode's instance count and the instancesPerScene / shareAcrossScenes
+ * uniforms (renderer/node.py:43-46,68,90-91; shaders/basic.vert:25-28).
+ * Nodes draw in the order they are added (the reference's draw order). */
+int pbr_node_add(pbr_ctx* ctx, int mesh_id, int instances_per_scene, int shared, int* out_node_id);
+
+/* Bind a node's per-instance device buffers (float32, B rows):
+ * d_pos [B,3], d_rot (see PBR_MODE_*), d_scale [B], d_color [B,4] RGBA.
+ * d_counts [N] int32 (optional, may be NULL): active instances of this node
+ * in scene k (0..instances_per_scene).  Replaces matbuf/colbuf uploads
+ * (renderer/node.py:110-178): the kernels build M = [R*s | t] themselves. */
+int pbr_node_set_buffers(pbr_ctx* ctx, int node_id, int mode, const float* d_pos, const float* d_rot,
+                         const float* d_scale, const float* d_color, const int32_t* d_counts);
+
+/* Bind the per-scene view-projection matrices d_vp [N,16] (row-major, GL
+ * clip-space conventions) and the camera's near/far planes (used by the soft
+ * mode's depth normalisation).  Replaces viewbuf (renderer/camera.py:146-148,
+ * 252-262) and tilebuf (camera.py:110-135): scene k renders into its own
+ * W x H image, which is what the tile viewport of shaders/basic.vert:45-52
+ * plus the discard of shaders/basic.frag:22-29 amount to. */
+int pbr_camera_bind(pbr_ctx* ctx, const float* d_vp, float z_near, float z_far);
+
+/* Lighting uniforms of shaders/basic.frag:13-18 (renderer/light.py:26-44):
+ * ambient colour, direction *towards* the light (normalised by the kernel),
+ * light colour, strength (clamped to [0,1]).  Before the first call the
+ * renderer is unlit (strength 0). */
+int pbr_light_set(pbr_ctx* ctx, const float ambient[3], const float direction[3], const float color[3],
+                  float strength);
+
+/* Clear colour (renderer/renderer.py:91-94,262); default (0,0,0,1). */
+int pbr_background_set(pbr_ctx* ctx, const float rgba[4]);
+
+/* Raster launch configuration: threads per CTA (128, 256 or 512), bin size in
+ * pixels (8, 16 or 32), triangle capacity per chunk (0 = automatic) and
+ * persistent work-stealing scheduling (0/1).  No counterpart in the
+ * reference (the GL driver schedules its own work). */
+int pbr_raster_config(pbr_ctx* ctx, int threads, int bin_px, int tri_cap, int persistent);
+
+/* Time the candidate launch configurations on the bound scene and keep the
+ * fastest.  d_out is an [N,C,H,W] uint8 scratch image.  Synchronises the
+ * stream; do not call during graph capture.  Reports the choice through the
+ * out pointers (any may be NULL).  No counterpart in the reference. */
+int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_threads, int* out_bin_px,
+                 int* out_tri_cap, int* out_persistent, float* out_ms);
+
+/* Render every scene (hard raster): d_out [N,C,H,W] uint8, optional
+ * d_depth [N,H,W] float32 window depth (1.0 where nothing is drawn) and
+ * optional d_winner [N,H,W] int32 (instance rank within the scene, counted
+ * in node order, times the largest mesh's triangle count plus the triangle
+ * index; -1 for background).  Replaces taskMgr.step() + grab_pixels +
+ * _rearrange_img (renderer/renderer.py:377-390,326-363). */
+int pbr_render(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, int32_t* d_winner, void* stream);
+
+/* "Plain" per-node path that mirrors the reference's per-step flow (one draw
+ * per node into a depth/colour buffer, then a readback into [N,C,H,W]):
+ * clear, draw one node, resolve.  Uses a context-owned colour+depth buffer
+ * allocated on first use (N*H*W*8 bytes). */
+int pbr_plain_clear(pbr_ctx* ctx, void* stream);
+int pbr_plain_draw(pbr_ctx* ctx, int node_id, void* stream);
+int pbr_plain_resolve(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, void* stream);
+
+/* Model matrices the kernels build for one node: d_out [B,16] row-major.
+ * For tests; replaces reading back matbuf (renderer/node.py:110-126). */
+int pbr_debug_transforms(pbr_ctx* ctx, int node_id, float* d_out, void* stream);
+
+/* Device-side error flags accumulated since the last call (synchronises the
+ * context's device, then clears them).  0 = none. */
+int pbr_device_status(pbr_ctx* ctx, int32_t* out_flags);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBR_CAPI_H */

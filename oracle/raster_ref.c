@@ -1,0 +1,640 @@
+/*
+ * raster_ref.c -- CPU restatement of pybatchrender's render path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle and the timed CPU
+ * baseline; the product renderer never links, loads or calls it.  Only tests/,
+ * __graft_entry__.smoke() and bench.py (its cpu_baseline leg and the
+ * "--impl reference" arm) use it.
+ *
+ * Built twice from this one source (see oracle/Makefile / oracle/build.py):
+ *   REAL=double  -> symbols *_f64  (the FP64 checker)
+ *   REAL=float   -> symbols *_f32  (the FP32 multithreaded CPU baseline)
+ *
+ * What it restates (paths relative to the reference project):
+ *   shaders/basic.vert:24-57     instance decode (scene = gid / I, inst = gid % I,
+ *                                id = shared ? inst : gid), clip = VP[scene] * M[id] * v,
+ *                                v_normal = normalize(mat3(M) * n), v_color = colbuf[id]
+ *   shaders/basic.frag:20-39     tile discard, base = 1 (useTexture = 0),
+ *                                ndl = max(dot(normalize(n), normalize(L)), 0),
+ *                                l = mix(1, ambient + ndl * col, clamp(strength, 0, 1)),
+ *                                rgb = color.rgb * l, a = color.a
+ *   renderer/shader_context.py:47-84  R = Rz(H) Ry(P) Rx(R), M = [R*s | t]
+ *   renderer/node.py:116-126     M[:3,:3] = rot3 * scale, M[:3,3] = position
+ *   renderer/camera.py:110-135 + shaders/basic.vert:45-52
+ *                                per-scene tile viewport; equivalent to rendering scene k
+ *                                into its own W x H image with the GL viewport transform
+ *   renderer/frame_grabber.py:105,167  vertical flip: image row 0 is the top row
+ *   renderer/renderer.py:352-363 scene order of the [N,C,H,W] output
+ *   renderer/renderer.py:262     clear colour (default black, alpha 1)
+ *
+ * The rasterisation rules are the GL contract the reference relies on through
+ * the OpenGL driver (not in the reference sources; the driver's own choices
+ * are not pinned by any reference test): pixel centres at +0.5, triangles
+ * clipped against the near plane (z_clip >= -w_clip), back faces culled
+ * (Panda3D's default cull mode: counter-clockwise front faces in GL window
+ * coordinates), top-left fill rule, depth test strict-less against a 1.0
+ * clear, equal depths resolved by draw order (node, then instance, then
+ * triangle), window depth = 0.5 * z_ndc + 0.5, screen-linear depth and
+ * perspective-correct normal interpolation, UNORM8 = floor(clamp(c,0,1)*255+0.5).
+ */
+#include <math.h>
+#include <tgmath.h> /* sin/cos/sqrt/exp follow REAL: float math in the FP32 build */
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifndef REAL
+#define REAL double
+#endif
+#ifndef SFX
+#define SFX _f64
+#endif
+#define CAT_(a, b) a##b
+#define CAT(a, b) CAT_(a, b)
+#define FN(name) CAT(name, SFX)
+
+typedef REAL real;
+
+#define ORC_MODE_HPR 0
+#define ORC_MODE_ROT 1
+#define ORC_MODE_MAT 2
+
+typedef struct {
+    int32_t nv, nt;
+    const float* pos;    /* [nv*3] */
+    const float* nrm;    /* [nv*3] */
+    const int32_t* idx;  /* [nt*3] */
+} orc_mesh;
+
+typedef struct {
+    int32_t mesh;
+    int32_t inst_per_scene; /* I */
+    int32_t shared;         /* 1: instance i of every scene reads buffer row i */
+    int32_t mode;           /* ORC_MODE_* */
+    const int32_t* counts;  /* [N] active instances per scene, or NULL (= I) */
+    const float* pos;       /* [B*3] */
+    const float* rot;       /* HPR [B*3] radians | ROT [B*9] | MAT [B*16] row-major */
+    const float* scale;     /* [B] (ignored for MAT) */
+    const float* color;     /* [B*4] */
+} orc_node;
+
+typedef struct {
+    int32_t N, W, H, C;
+    const float* vp;        /* [N*16] row-major view-projection per scene */
+    float ambient[3], ldir[3], lcol[3], strength;
+    float bg[4];
+    int32_t cull;           /* 1: cull back faces (default) */
+    /* soft mode */
+    float znear, zfar, sigma, gamma;
+    int32_t soft_dense;     /* 1: no coverage cutoff (every triangle reaches every pixel) */
+} orc_scene;
+
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    real m[12];             /* 3x4 row-major affine model matrix */
+    real c[4];              /* colour */
+} inst_xf;
+
+static void build_instance(const orc_node* nd, int64_t id, inst_xf* out) {
+    real R[9];
+    const float* p = nd->pos + id * 3;
+    if (nd->mode == ORC_MODE_MAT) {
+        const float* mm = nd->rot + id * 16;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 4; ++c) out->m[r * 4 + c] = (real)mm[r * 4 + c];
+    } else {
+        if (nd->mode == ORC_MODE_HPR) {
+            const float* a = nd->rot + id * 3;
+            real h = a[0], pp = a[1], rr = a[2];
+            real ch = cos(h), sh = sin(h), cp = cos(pp), sp = sin(pp), cr = cos(rr), sr = sin(rr);
+            /* Rz(H) @ Ry(P) @ Rx(R), renderer/shader_context.py:63-82 */
+            R[0] = ch * cp; R[1] = ch * sp * sr - sh * cr; R[2] = ch * sp * cr + sh * sr;
+            R[3] = sh * cp; R[4] = sh * sp * sr + ch * cr; R[5] = sh * sp * cr - ch * sr;
+            R[6] = -sp;     R[7] = cp * sr;                R[8] = cp * cr;
+        } else {
+            const float* a = nd->rot + id * 9;
+            for (int i = 0; i < 9; ++i) R[i] = a[i];
+        }
+        real s = nd->scale[id];
+        for (int r = 0; r < 3; ++r) {
+            for (int c = 0; c < 3; ++c) out->m[r * 4 + c] = R[r * 3 + c] * s;
+            out->m[r * 4 + 3] = p[r];
+        }
+    }
+    for (int i = 0; i < 4; ++i) out->c[i] = nd->color[id * 4 + i];
+}
+
+typedef struct {
+    real x, y, z, w;        /* clip coordinates */
+    real n[3];              /* world normal (normalised, basic.vert:53) */
+} cvert;
+
+static void xform_vertex(const inst_xf* xf, const real* VP, const float* p, const float* n, cvert* o) {
+    real wx = xf->m[0] * p[0] + xf->m[1] * p[1] + xf->m[2] * p[2] + xf->m[3];
+    real wy = xf->m[4] * p[0] + xf->m[5] * p[1] + xf->m[6] * p[2] + xf->m[7];
+    real wz = xf->m[8] * p[0] + xf->m[9] * p[1] + xf->m[10] * p[2] + xf->m[11];
+    o->x = VP[0] * wx + VP[1] * wy + VP[2] * wz + VP[3];
+    o->y = VP[4] * wx + VP[5] * wy + VP[6] * wz + VP[7];
+    o->z = VP[8] * wx + VP[9] * wy + VP[10] * wz + VP[11];
+    o->w = VP[12] * wx + VP[13] * wy + VP[14] * wz + VP[15];
+    real nx = xf->m[0] * n[0] + xf->m[1] * n[1] + xf->m[2] * n[2];
+    real ny = xf->m[4] * n[0] + xf->m[5] * n[1] + xf->m[6] * n[2];
+    real nz = xf->m[8] * n[0] + xf->m[9] * n[1] + xf->m[10] * n[2];
+    real ln = sqrt(nx * nx + ny * ny + nz * nz);
+    real inv = ln > 0 ? (real)1 / ln : (real)0;
+    o->n[0] = nx * inv; o->n[1] = ny * inv; o->n[2] = nz * inv;
+}
+
+/* Clip a triangle against the near plane z + w >= 0 (Sutherland-Hodgman).
+ * Returns the vertex count of the clipped polygon (0, 3 or 4). */
+static int clip_near(const cvert* in, cvert* out) {
+    int n = 0;
+    for (int i = 0; i < 3; ++i) {
+        const cvert* a = &in[i];
+        const cvert* b = &in[(i + 1) % 3];
+        real da = a->z + a->w, db = b->z + b->w;
+        if (da >= 0) out[n++] = *a;
+        if ((da >= 0) != (db >= 0)) {
+            real t = da / (da - db);
+            cvert v;
+            v.x = a->x + t * (b->x - a->x);
+            v.y = a->y + t * (b->y - a->y);
+            v.z = a->z + t * (b->z - a->z);
+            v.w = a->w + t * (b->w - a->w);
+            for (int k = 0; k < 3; ++k) v.n[k] = a->n[k] + t * (b->n[k] - a->n[k]);
+            out[n++] = v;
+        }
+    }
+    return n;
+}
+
+typedef struct {
+    real sx[3], sy[3], sz[3], iw[3];   /* screen x, y (pixels, y down), window depth, 1/w */
+    real n[3][3];
+    real A[3], B[3], Cc[3];            /* edge functions, edge k opposite vertex k */
+    int tl[3];
+    real area2;
+    int x0, x1, y0, y1;                /* inclusive pixel bbox, clamped */
+} stri;
+
+/* Edge k runs from vertex (k+1)%3 to (k+2)%3; E_k(p) = A p.x + B p.y + C is
+ * positive on the triangle's side and equals area2 * barycentric_k. */
+static void setup_edges(stri* t) {
+    for (int k = 0; k < 3; ++k) {
+        int a = (k + 1) % 3, b = (k + 2) % 3;
+        t->A[k] = t->sy[a] - t->sy[b];
+        t->B[k] = t->sx[b] - t->sx[a];
+        t->Cc[k] = -(t->A[k] * t->sx[a] + t->B[k] * t->sy[a]);
+        /* top-left rule in image coordinates (y down) */
+        t->tl[k] = (t->A[k] > 0) || (t->A[k] == 0 && t->B[k] > 0);
+    }
+}
+
+/* Screen-space setup of one clipped triangle.  Returns 0 when it is culled. */
+static int setup_tri(const orc_scene* sc, const cvert* v0, const cvert* v1, const cvert* v2, stri* t) {
+    const cvert* v[3] = {v0, v1, v2};
+    for (int k = 0; k < 3; ++k) {
+        real iw = (real)1 / v[k]->w;
+        t->sx[k] = (v[k]->x * iw + 1) * (real)0.5 * sc->W;
+        t->sy[k] = (1 - v[k]->y * iw) * (real)0.5 * sc->H;
+        t->sz[k] = v[k]->z * iw * (real)0.5 + (real)0.5;
+        t->iw[k] = iw;
+        for (int c = 0; c < 3; ++c) t->n[k][c] = v[k]->n[c];
+    }
+    real area2 = (t->sx[1] - t->sx[0]) * (t->sy[2] - t->sy[0]) - (t->sx[2] - t->sx[0]) * (t->sy[1] - t->sy[0]);
+    /* GL front faces are counter-clockwise with y up, i.e. area2 < 0 with y down */
+    if (area2 == 0) return 0;
+    if (area2 > 0) {
+        if (sc->cull) return 0;
+    }
+    if (area2 < 0) {
+        /* swap vertices 1 and 2 so that the interior is on the positive side */
+        real tmp;
+#define SWP(a, b) (tmp = (a), (a) = (b), (b) = tmp)
+        SWP(t->sx[1], t->sx[2]); SWP(t->sy[1], t->sy[2]); SWP(t->sz[1], t->sz[2]); SWP(t->iw[1], t->iw[2]);
+        for (int c = 0; c < 3; ++c) SWP(t->n[1][c], t->n[2][c]);
+#undef SWP
+        area2 = -area2;
+    }
+    t->area2 = area2;
+    setup_edges(t);
+    real mnx = t->sx[0], mxx = t->sx[0], mny = t->sy[0], mxy = t->sy[0];
+    for (int k = 1; k < 3; ++k) {
+        if (t->sx[k] < mnx) mnx = t->sx[k];
+        if (t->sx[k] > mxx) mxx = t->sx[k];
+        if (t->sy[k] < mny) mny = t->sy[k];
+        if (t->sy[k] > mxy) mxy = t->sy[k];
+    }
+    /* pixels whose centre (x+0.5) can lie in [mn, mx], widened by one pixel */
+    real fx0 = floor(mnx - (real)0.5) - 1, fx1 = ceil(mxx - (real)0.5) + 1;
+    real fy0 = floor(mny - (real)0.5) - 1, fy1 = ceil(mxy - (real)0.5) + 1;
+    if (fx1 < 0 || fy1 < 0 || fx0 > sc->W - 1 || fy0 > sc->H - 1) return 0;
+    t->x0 = fx0 < 0 ? 0 : (int)fx0;
+    t->y0 = fy0 < 0 ? 0 : (int)fy0;
+    t->x1 = fx1 > sc->W - 1 ? sc->W - 1 : (int)fx1;
+    t->y1 = fy1 > sc->H - 1 ? sc->H - 1 : (int)fy1;
+    return 1;
+}
+
+static inline int covers(const stri* t, const real E[3]) {
+    for (int k = 0; k < 3; ++k) {
+        if (E[k] > 0) continue;
+        if (E[k] == 0 && t->tl[k]) continue;
+        return 0;
+    }
+    return 1;
+}
+
+static inline real clamp01(real v) { return v < 0 ? 0 : (v > 1 ? 1 : v); }
+
+static inline uint8_t to_unorm8(real v) {
+    return (uint8_t)floor(clamp01(v) * (real)255 + (real)0.5);
+}
+
+/* basic.frag:33-38 for a world normal n (not yet normalised). */
+static void shade(const orc_scene* sc, const real Ln[3], const real n_in[3], const real col[4], real out[4]) {
+    real ln = sqrt(n_in[0] * n_in[0] + n_in[1] * n_in[1] + n_in[2] * n_in[2]);
+    real inv = ln > 0 ? (real)1 / ln : (real)0;
+    real ndl = (n_in[0] * Ln[0] + n_in[1] * Ln[1] + n_in[2] * Ln[2]) * inv;
+    if (!(ndl > 0)) ndl = 0;
+    real s = clamp01((real)sc->strength);
+    for (int c = 0; c < 3; ++c) {
+        real light = (real)sc->ambient[c] + ndl * (real)sc->lcol[c];
+        real l = (real)1 * (1 - s) + light * s;
+        out[c] = col[c] * l;
+    }
+    out[3] = col[3];
+}
+
+static void light_dir(const orc_scene* sc, real Ln[3]) {
+    real lx = sc->ldir[0], ly = sc->ldir[1], lz = sc->ldir[2];
+    real ln = sqrt(lx * lx + ly * ly + lz * lz);
+    real inv = ln > 0 ? (real)1 / ln : (real)0;
+    Ln[0] = lx * inv; Ln[1] = ly * inv; Ln[2] = lz * inv;
+}
+
+/* Walk every triangle of scene k in draw order.  The callback receives the
+ * screen triangle, its instance colour and its winner id. */
+typedef void (*tri_cb)(void* user, const stri* t, const real col[4], int32_t wid);
+
+static int scene_max_tris(int nmeshes, const orc_mesh* meshes) {
+    int mt = 1;
+    for (int i = 0; i < nmeshes; ++i)
+        if (meshes[i].nt > mt) mt = meshes[i].nt;
+    return mt;
+}
+
+static void walk_scene(const orc_scene* sc, int nmeshes, const orc_mesh* meshes, int nnodes,
+                       const orc_node* nodes, int k, int soft, tri_cb cb, void* user) {
+    real VP[16];
+    for (int i = 0; i < 16; ++i) VP[i] = sc->vp[(int64_t)k * 16 + i];
+    int max_tris = scene_max_tris(nmeshes, meshes);
+    int rank_base = 0;
+    cvert* cache = NULL;
+    int cache_cap = 0;
+    for (int n = 0; n < nnodes; ++n) {
+        const orc_node* nd = &nodes[n];
+        const orc_mesh* me = &meshes[nd->mesh];
+        int ips = nd->inst_per_scene;
+        int cnt = nd->counts ? nd->counts[k] : ips;
+        if (cnt > ips) cnt = ips;
+        if (me->nv > cache_cap) {
+            free(cache);
+            cache_cap = me->nv;
+            cache = (cvert*)malloc(sizeof(cvert) * (size_t)cache_cap);
+        }
+        for (int i = 0; i < cnt; ++i) {
+            int64_t id = nd->shared ? (int64_t)i : (int64_t)k * ips + i;
+            inst_xf xf;
+            build_instance(nd, id, &xf);
+            for (int v = 0; v < me->nv; ++v)
+                xform_vertex(&xf, VP, me->pos + 3 * v, me->nrm + 3 * v, &cache[v]);
+            int32_t wid_base = (int32_t)((rank_base + i) * max_tris);
+            for (int t = 0; t < me->nt; ++t) {
+                cvert tv[3];
+                for (int c = 0; c < 3; ++c) tv[c] = cache[me->idx[3 * t + c]];
+                cvert poly[4];
+                int np;
+                if (soft) {
+                    /* soft mode drops triangles that are not fully in front of the near plane */
+                    if (tv[0].z + tv[0].w < 0 || tv[1].z + tv[1].w < 0 || tv[2].z + tv[2].w < 0) continue;
+                    for (int c = 0; c < 3; ++c) poly[c] = tv[c];
+                    np = 3;
+                } else {
+                    np = clip_near(tv, poly);
+                }
+                for (int f = 1; f + 1 < np; ++f) {
+                    stri st;
+                    if (!setup_tri(sc, &poly[0], &poly[f], &poly[f + 1], &st)) continue;
+                    cb(user, &st, xf.c, wid_base + t);
+                }
+            }
+        }
+        rank_base += ips;
+    }
+    free(cache);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Hard raster                                                               */
+
+typedef struct {
+    const orc_scene* sc;
+    real Ln[3];
+    real* zbuf;       /* [H*W] */
+    real* rgba;       /* [H*W*4] */
+    int32_t* win;     /* [H*W] */
+    uint8_t* amb;     /* [H*W] or NULL */
+    real tol_px, tol_z;
+} hard_ctx;
+
+static void hard_pass1(void* user, const stri* t, const real col[4], int32_t wid) {
+    hard_ctx* h = (hard_ctx*)user;
+    const orc_scene* sc = h->sc;
+    for (int y = t->y0; y <= t->y1; ++y) {
+        real py = y + (real)0.5;
+        for (int x = t->x0; x <= t->x1; ++x) {
+            real px = x + (real)0.5;
+            real E[3];
+            for (int k = 0; k < 3; ++k) E[k] = t->A[k] * px + t->B[k] * py + t->Cc[k];
+            if (!covers(t, E)) continue;
+            real b0 = E[0] / t->area2, b1 = E[1] / t->area2, b2 = E[2] / t->area2;
+            real z = b0 * t->sz[0] + b1 * t->sz[1] + b2 * t->sz[2];
+            if (z < 0) z = 0; /* GL clamps window depth to [0,1] */
+            int64_t o = (int64_t)y * sc->W + x;
+            if (!(z < h->zbuf[o])) continue;
+            h->zbuf[o] = z;
+            h->win[o] = wid;
+            /* perspective-correct normal (basic.frag:33) */
+            real q0 = b0 * t->iw[0], q1 = b1 * t->iw[1], q2 = b2 * t->iw[2];
+            real qs = q0 + q1 + q2;
+            real nn[3];
+            for (int c = 0; c < 3; ++c) nn[c] = (q0 * t->n[0][c] + q1 * t->n[1][c] + q2 * t->n[2][c]) / qs;
+            shade(sc, h->Ln, nn, col, &h->rgba[o * 4]);
+        }
+    }
+}
+
+/* Second walk: flag pixels whose centre lies within tol_px of an edge of a
+ * triangle that is (nearly) visible there, or that another covering
+ * fragment ties in depth within tol_z. */
+static void hard_pass2(void* user, const stri* t, const real col[4], int32_t wid) {
+    (void)col;
+    hard_ctx* h = (hard_ctx*)user;
+    const orc_scene* sc = h->sc;
+    real L[3];
+    for (int k = 0; k < 3; ++k) L[k] = sqrt(t->A[k] * t->A[k] + t->B[k] * t->B[k]);
+    for (int y = t->y0; y <= t->y1; ++y) {
+        real py = y + (real)0.5;
+        for (int x = t->x0; x <= t->x1; ++x) {
+            real px = x + (real)0.5;
+            real E[3], dmin = 1e30;
+            for (int k = 0; k < 3; ++k) {
+                E[k] = t->A[k] * px + t->B[k] * py + t->Cc[k];
+                real d = L[k] > 0 ? E[k] / L[k] : 0;
+                if (d < dmin) dmin = d;
+            }
+            real b0 = E[0] / t->area2, b1 = E[1] / t->area2, b2 = E[2] / t->area2;
+            real z = b0 * t->sz[0] + b1 * t->sz[1] + b2 * t->sz[2];
+            if (z < 0) z = 0;
+            int64_t o = (int64_t)y * sc->W + x;
+            real zb = h->zbuf[o];
+            if (fabs(dmin) < h->tol_px && z <= zb + h->tol_z && z < 1) h->amb[o] = 1;
+            if (covers(t, E) && h->win[o] != wid && fabs(z - zb) < h->tol_z) h->amb[o] = 1;
+        }
+    }
+}
+
+typedef struct {
+    const orc_scene* sc;
+    int nmeshes;
+    const orc_mesh* meshes;
+    int nnodes;
+    const orc_node* nodes;
+    uint8_t* out;
+    float* depth;
+    int32_t* winner;
+    uint8_t* ambiguous;
+    real tol_px, tol_z;
+    int k0, k1;
+    int status;
+} hard_job;
+
+static void* hard_worker(void* arg) {
+    hard_job* j = (hard_job*)arg;
+    const orc_scene* sc = j->sc;
+    int64_t P = (int64_t)sc->W * sc->H;
+    hard_ctx h;
+    h.sc = sc;
+    light_dir(sc, h.Ln);
+    h.zbuf = (real*)malloc(sizeof(real) * P);
+    h.rgba = (real*)malloc(sizeof(real) * P * 4);
+    h.win = (int32_t*)malloc(sizeof(int32_t) * P);
+    h.amb = j->ambiguous ? (uint8_t*)malloc((size_t)P) : NULL;
+    h.tol_px = j->tol_px;
+    h.tol_z = j->tol_z;
+    if (!h.zbuf || !h.rgba || !h.win || (j->ambiguous && !h.amb)) {
+        j->status = -1;
+        free(h.zbuf); free(h.rgba); free(h.win); free(h.amb);
+        return NULL;
+    }
+    for (int k = j->k0; k < j->k1; ++k) {
+        for (int64_t o = 0; o < P; ++o) {
+            h.zbuf[o] = 1;
+            h.win[o] = -1;
+            for (int c = 0; c < 4; ++c) h.rgba[o * 4 + c] = sc->bg[c];
+        }
+        walk_scene(sc, j->nmeshes, j->meshes, j->nnodes, j->nodes, k, 0, hard_pass1, &h);
+        if (h.amb) {
+            memset(h.amb, 0, (size_t)P);
+            walk_scene(sc, j->nmeshes, j->meshes, j->nnodes, j->nodes, k, 0, hard_pass2, &h);
+            memcpy(j->ambiguous + (int64_t)k * P, h.amb, (size_t)P);
+        }
+        for (int c = 0; c < sc->C; ++c) {
+            uint8_t* dst = j->out + ((int64_t)k * sc->C + c) * P;
+            for (int64_t o = 0; o < P; ++o) dst[o] = to_unorm8(h.rgba[o * 4 + c]);
+        }
+        if (j->depth)
+            for (int64_t o = 0; o < P; ++o) j->depth[(int64_t)k * P + o] = (float)h.zbuf[o];
+        if (j->winner) memcpy(j->winner + (int64_t)k * P, h.win, sizeof(int32_t) * P);
+    }
+    free(h.zbuf); free(h.rgba); free(h.win); free(h.amb);
+    return NULL;
+}
+
+/* Render scenes [k0, k1) into out[N,C,H,W] (scene-indexed; only the rows of
+ * the requested scenes are written).  depth [N,H,W], winner [N,H,W] and
+ * ambiguous [N,H,W] may be NULL.  Winner id = instance rank within the scene
+ * (node-major) * max_triangles + triangle index, -1 for background. */
+int FN(orc_render_hard)(const orc_scene* sc, int nmeshes, const orc_mesh* meshes, int nnodes,
+                        const orc_node* nodes, int k0, int k1, uint8_t* out, float* depth,
+                        int32_t* winner, uint8_t* ambiguous, float tol_px, float tol_z,
+                        int nthreads) {
+    if (!sc || !out || sc->W <= 0 || sc->H <= 0 || sc->C < 1 || sc->C > 4) return -2;
+    if (k0 < 0 || k1 > sc->N || k0 > k1) return -2;
+    if (nthreads < 1) nthreads = 1;
+    int nscenes = k1 - k0;
+    if (nthreads > nscenes) nthreads = nscenes > 0 ? nscenes : 1;
+    hard_job* jobs = (hard_job*)calloc((size_t)nthreads, sizeof(hard_job));
+    pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    for (int i = 0; i < nthreads; ++i) {
+        hard_job* j = &jobs[i];
+        j->sc = sc; j->nmeshes = nmeshes; j->meshes = meshes; j->nnodes = nnodes; j->nodes = nodes;
+        j->out = out; j->depth = depth; j->winner = winner; j->ambiguous = ambiguous;
+        j->tol_px = tol_px; j->tol_z = tol_z;
+        j->k0 = k0 + (int)((int64_t)nscenes * i / nthreads);
+        j->k1 = k0 + (int)((int64_t)nscenes * (i + 1) / nthreads);
+    }
+    int rc = 0;
+    if (nthreads == 1) {
+        hard_worker(&jobs[0]);
+    } else {
+        for (int i = 0; i < nthreads; ++i) pthread_create(&th[i], NULL, hard_worker, &jobs[i]);
+        for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    }
+    for (int i = 0; i < nthreads; ++i)
+        if (jobs[i].status) rc = jobs[i].status;
+    free(jobs);
+    free(th);
+    return rc;
+}
+
+/* Model matrices as the renderer builds them: out [B,16] row-major 4x4. */
+int FN(orc_instance_matrices)(const orc_node* nd, int64_t B, float* out) {
+    for (int64_t id = 0; id < B; ++id) {
+        inst_xf xf;
+        build_instance(nd, id, &xf);
+        for (int i = 0; i < 12; ++i) out[id * 16 + i] = (float)xf.m[i];
+        out[id * 16 + 12] = 0; out[id * 16 + 13] = 0; out[id * 16 + 14] = 0; out[id * 16 + 15] = 1;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Soft coverage (differentiable mode)                                       */
+/*
+ * Per fragment (pixel p, front-facing triangle j fully in front of the near plane):
+ *   e_k   = E_k(p) / |(A_k, B_k)|              signed distance to edge line k (px)
+ *   D_j   = prod_k sigmoid(e_k / sigma)        soft coverage; 0 when min_k e_k < -16 sigma
+ *                                              (unless soft_dense)
+ *   1/w   = sum_k b_k / w_k                    b_k = E_k / area2 (unclamped)
+ *   zs_j  = (zfar - w) / (zfar - znear)        normalised linear depth, nearer = larger
+ *   C_j   = basic.frag shading with the perspective-correct (extrapolated) normal,
+ *           unclamped
+ *   w_j   = D_j exp((zs_j - max zs) / gamma)
+ *   A     = 1 - prod_j (1 - D_j)
+ *   out   = A * sum_j w_j C_j / sum_j w_j + (1 - A) * bg.rgb
+ */
+
+typedef struct {
+    const orc_scene* sc;
+    real Ln[3];
+    real* m;      /* running max zs  [P] */
+    real* S;      /* sum of weights  [P] */
+    real* acc;    /* weighted colour [P*3] */
+    real* Pi;     /* prod (1 - D)    [P] */
+} soft_ctx;
+
+#define SOFT_CUTOFF 16.0
+
+static void soft_cb(void* user, const stri* t, const real col[4], int32_t wid) {
+    (void)wid;
+    soft_ctx* s = (soft_ctx*)user;
+    const orc_scene* sc = s->sc;
+    real sig = sc->sigma;
+    real L[3];
+    for (int k = 0; k < 3; ++k) L[k] = sqrt(t->A[k] * t->A[k] + t->B[k] * t->B[k]);
+    int x0, x1, y0, y1;
+    if (sc->soft_dense) {
+        x0 = 0; y0 = 0; x1 = sc->W - 1; y1 = sc->H - 1;
+    } else {
+        /* bbox widened by the cutoff distance */
+        real mnx = t->sx[0], mxx = t->sx[0], mny = t->sy[0], mxy = t->sy[0];
+        for (int k = 1; k < 3; ++k) {
+            if (t->sx[k] < mnx) mnx = t->sx[k];
+            if (t->sx[k] > mxx) mxx = t->sx[k];
+            if (t->sy[k] < mny) mny = t->sy[k];
+            if (t->sy[k] > mxy) mxy = t->sy[k];
+        }
+        real r = SOFT_CUTOFF * sig + 1;
+        real fx0 = floor(mnx - r), fx1 = ceil(mxx + r), fy0 = floor(mny - r), fy1 = ceil(mxy + r);
+        if (fx1 < 0 || fy1 < 0 || fx0 > sc->W - 1 || fy0 > sc->H - 1) return;
+        x0 = fx0 < 0 ? 0 : (int)fx0;
+        y0 = fy0 < 0 ? 0 : (int)fy0;
+        x1 = fx1 > sc->W - 1 ? sc->W - 1 : (int)fx1;
+        y1 = fy1 > sc->H - 1 ? sc->H - 1 : (int)fy1;
+    }
+    for (int y = y0; y <= y1; ++y) {
+        real py = y + (real)0.5;
+        for (int x = x0; x <= x1; ++x) {
+            real px = x + (real)0.5;
+            real E[3], e[3], emin = 1e30;
+            for (int k = 0; k < 3; ++k) {
+                E[k] = t->A[k] * px + t->B[k] * py + t->Cc[k];
+                e[k] = E[k] / L[k];
+                if (e[k] < emin) emin = e[k];
+            }
+            if (!sc->soft_dense && emin < -SOFT_CUTOFF * sig) continue;
+            real D = 1;
+            for (int k = 0; k < 3; ++k) D *= (real)1 / (1 + exp(-e[k] / sig));
+            real b0 = E[0] / t->area2, b1 = E[1] / t->area2, b2 = E[2] / t->area2;
+            real q0 = b0 * t->iw[0], q1 = b1 * t->iw[1], q2 = b2 * t->iw[2];
+            real qs = q0 + q1 + q2;
+            if (!(qs > 0)) continue;
+            real w = (real)1 / qs;
+            real zs = ((real)sc->zfar - w) / ((real)sc->zfar - (real)sc->znear);
+            real nn[3], C[4];
+            for (int c = 0; c < 3; ++c) nn[c] = (q0 * t->n[0][c] + q1 * t->n[1][c] + q2 * t->n[2][c]) * w;
+            shade(sc, s->Ln, nn, col, C);
+            int64_t o = (int64_t)y * sc->W + x;
+            s->Pi[o] *= (1 - D);
+            if (zs > s->m[o]) {
+                real f = exp((s->m[o] - zs) / (real)sc->gamma);
+                s->S[o] = s->S[o] * f + D;
+                for (int c = 0; c < 3; ++c) s->acc[o * 3 + c] = s->acc[o * 3 + c] * f + D * C[c];
+                s->m[o] = zs;
+            } else {
+                real f = D * exp((zs - s->m[o]) / (real)sc->gamma);
+                s->S[o] += f;
+                for (int c = 0; c < 3; ++c) s->acc[o * 3 + c] += f * C[c];
+            }
+        }
+    }
+}
+
+/* Soft render of scenes [k0,k1) into out[N,3,H,W] (float). */
+int FN(orc_render_soft)(const orc_scene* sc, int nmeshes, const orc_mesh* meshes, int nnodes,
+                        const orc_node* nodes, int k0, int k1, float* out) {
+    if (!sc || !out || k0 < 0 || k1 > sc->N || k0 > k1) return -2;
+    int64_t P = (int64_t)sc->W * sc->H;
+    soft_ctx s;
+    s.sc = sc;
+    light_dir(sc, s.Ln);
+    s.m = (real*)malloc(sizeof(real) * P);
+    s.S = (real*)malloc(sizeof(real) * P);
+    s.acc = (real*)malloc(sizeof(real) * P * 3);
+    s.Pi = (real*)malloc(sizeof(real) * P);
+    if (!s.m || !s.S || !s.acc || !s.Pi) {
+        free(s.m); free(s.S); free(s.acc); free(s.Pi);
+        return -1;
+    }
+    for (int k = k0; k < k1; ++k) {
+        for (int64_t o = 0; o < P; ++o) {
+            s.m[o] = -1e30; s.S[o] = 0; s.Pi[o] = 1;
+            s.acc[o * 3] = s.acc[o * 3 + 1] = s.acc[o * 3 + 2] = 0;
+        }
+        walk_scene(sc, nmeshes, meshes, nnodes, nodes, k, 1, soft_cb, &s);
+        for (int c = 0; c < 3; ++c) {
+            float* dst = out + ((int64_t)k * 3 + c) * P;
+            for (int64_t o = 0; o < P; ++o) {
+                real A = 1 - s.Pi[o];
+                real fg = s.S[o] > 0 ? s.acc[o * 3 + c] / s.S[o] : 0;
+                dst[o] = (float)(A * fg + (1 - A) * (real)sc->bg[c]);
+            }
+        }
+    }
+    free(s.m); free(s.S); free(s.acc); free(s.Pi);
+    return 0;
+}

@@ -1,0 +1,531 @@
+// pbr_capi.cu -- implementation of include/pbr_capi.h.
+//
+// The context holds the host copy of the kernel parameters (SceneParams) and
+// the launch configuration; every render call derives RasterArgs from it and
+// enqueues kernels on the caller's stream.  The context owns only scratch: a
+// work counter and status word for the persistent schedule, and the colour /
+// depth buffer of the plain per-node path.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pbr_capi.h"
+#include "pbr_launch.h"
+
+using pbr::MeshDesc;
+using pbr::NodeDesc;
+using pbr::RasterArgs;
+using pbr::SceneParams;
+
+struct pbr_ctx {
+  int device = 0;
+  int sm_count = 1;
+  int max_smem = 48 * 1024;
+  std::string err;
+  SceneParams P;
+  std::vector<bool> node_ready;
+  bool cam_bound = false;
+  // launch configuration
+  int threads = 256;
+  int bin_px = 16;
+  int tri_cap_req = 0;
+  int persistent = 0;
+  // scratch
+  int32_t* d_counter = nullptr;
+  int32_t* d_status = nullptr;
+  float* d_zbuf = nullptr;
+  uint32_t* d_cbuf = nullptr;
+  // cudaFuncSetAttribute cache: [threads idx][plain][winner]
+  int smem_set[3][2][2] = {};
+};
+
+static thread_local std::string g_create_err;
+
+static int set_err(pbr_ctx* ctx, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf; else g_create_err = buf;
+  return code;
+}
+
+static int cuda_err(pbr_ctx* ctx, cudaError_t e, const char* what) {
+  return set_err(ctx, PBR_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define PBR_CHECK_CTX(ctx) \
+  do { if (!(ctx)) { g_create_err = "null context"; return PBR_ERR_INVALID; } } while (0)
+
+static int threads_index(int t) { return t == 128 ? 0 : (t == 256 ? 1 : 2); }
+
+static uint32_t pack_bg(const float* c) {
+  uint32_t v = 0;
+  for (int i = 0; i < 4; ++i) {
+    float x = std::min(std::max(c[i], 0.f), 1.f);
+    uint32_t b = (uint32_t)std::floor(x * 255.f + 0.5f);
+    v |= b << (8 * i);
+  }
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// launch configuration
+
+struct LaunchPlan {
+  RasterArgs A;
+  int smem = 0;
+  int grid = 0;
+};
+
+static long long scene_source_tris(const pbr_ctx* ctx, int n0, int n1) {
+  long long s = 0;
+  for (int n = n0; n < n1; ++n) {
+    const NodeDesc& nd = ctx->P.nodes[n];
+    s += (long long)nd.ips * ctx->P.meshes[nd.mesh].nt;
+  }
+  return s;
+}
+
+static int plan_launch(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int persistent, bool plain,
+                       bool winner, int n0, int n1, LaunchPlan* out) {
+  const SceneParams& P = ctx->P;
+  RasterArgs A;
+  memset(&A, 0, sizeof(A));
+  const int HW = P.W * P.H;
+  A.node_begin = n0;
+  A.node_end = n1;
+  A.bin_px = bin_px;
+  A.bins_x = (P.W + bin_px - 1) / bin_px;
+  A.region_px = threads * pbr::kPx;
+  A.regions_per_scene = (HW + A.region_px - 1) / A.region_px;
+  A.num_items = P.N * A.regions_per_scene;
+  int mrb = 1;
+  for (int r = 0; r < A.regions_per_scene; ++r) {
+    const int p0 = r * A.region_px, p1 = std::min(p0 + A.region_px, HW);
+    const int rb = ((p1 - 1) / P.W) / bin_px - (p0 / P.W) / bin_px + 1;
+    mrb = std::max(mrb, rb);
+  }
+  A.max_region_bins = mrb * A.bins_x;
+  int max_nv = 1;
+  long long max_inst_verts = 1;
+  for (int n = n0; n < n1; ++n) {
+    const NodeDesc& nd = P.nodes[n];
+    const MeshDesc& me = P.meshes[nd.mesh];
+    max_nv = std::max(max_nv, me.nv);
+    max_inst_verts = std::max(max_inst_verts, (long long)nd.ips * me.nv);
+    if (me.smooth) A.smooth_any = 1;
+  }
+  A.vcap = std::max(max_nv, (int)std::min<long long>(max_inst_verts, 1024));
+  A.vcap = (A.vcap + 31) & ~31;
+  int icap = 1;
+  for (int n = n0; n < n1; ++n) {
+    const NodeDesc& nd = P.nodes[n];
+    icap = std::max(icap, std::min(nd.ips, A.vcap / std::max(1, P.meshes[nd.mesh].nv)));
+  }
+  A.icap = std::min(icap, 256);
+  const long long need = 2 * scene_source_tris(ctx, n0, n1);
+  int cap = tri_cap_req > 0 ? tri_cap_req : (int)std::min<long long>(std::max<long long>(need, 64), 1024);
+  cap = std::max(64, (cap + 31) & ~31);
+  A.persistent = persistent;
+  A.out = nullptr;
+  A.work_counter = ctx->d_counter;
+  A.status = ctx->d_status;
+  // shrink the chunk until the layout fits in shared memory
+  for (;;) {
+    A.tri_cap = cap;
+    A.multi_chunk = need > cap ? 1 : 0;
+    const pbr::SmemLayout L = pbr::smem_layout(A, threads, winner);
+    if (L.total <= ctx->max_smem) {
+      out->smem = L.total;
+      break;
+    }
+    if (cap > 64) {
+      cap = std::max(64, (cap / 2 + 31) & ~31);
+      continue;
+    }
+    if (A.vcap > max_nv) {
+      A.vcap = std::max(max_nv, A.vcap / 2);
+      A.icap = std::max(1, std::min(A.icap, A.vcap / max_nv));
+      continue;
+    }
+    return set_err(ctx, PBR_ERR_CAPACITY,
+                   "scene does not fit in shared memory (%d bytes needed, %d available); "
+                   "reduce mesh size or threads", L.total, ctx->max_smem);
+  }
+  // kernel attribute + occupancy
+  int& cached = ctx->smem_set[threads_index(threads)][plain ? 1 : 0][winner ? 1 : 0];
+  if (out->smem > 48 * 1024 && out->smem > cached) {
+    cudaError_t e = pbr::hard_set_smem_limit(threads, plain, winner, out->smem);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaFuncSetAttribute");
+    cached = out->smem;
+  }
+  if (persistent) {
+    int bps = 0;
+    cudaError_t e = pbr::hard_occupancy(threads, plain, winner, out->smem, &bps);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    out->grid = std::max(1, std::min(A.num_items, ctx->sm_count * std::max(1, bps)));
+  } else {
+    out->grid = A.num_items;
+  }
+  out->A = A;
+  return PBR_OK;
+}
+
+static int check_ready(pbr_ctx* ctx, int n0, int n1) {
+  if (!ctx->cam_bound) return set_err(ctx, PBR_ERR_STATE, "no camera bound (pbr_camera_bind)");
+  for (int n = n0; n < n1; ++n)
+    if (!ctx->node_ready[n]) return set_err(ctx, PBR_ERR_STATE, "node %d has no buffers bound", n);
+  long long ranks = 0;
+  for (int n = 0; n < ctx->P.num_nodes; ++n) ranks += ctx->P.nodes[n].ips;
+  if (ranks * (long long)ctx->P.max_tris >= (1LL << 31))
+    return set_err(ctx, PBR_ERR_CAPACITY, "instances per scene x triangles per mesh exceeds 2^31");
+  return PBR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+int pbr_version(void) { return 100; }
+
+const char* pbr_last_error(const pbr_ctx* ctx) {
+  if (!ctx) return g_create_err.c_str();
+  return ctx->err.c_str();
+}
+
+int pbr_create(pbr_ctx** out_ctx, int num_scenes, int width, int height, int channels, int flags) {
+  if (!out_ctx) return set_err(nullptr, PBR_ERR_INVALID, "out_ctx is null");
+  *out_ctx = nullptr;
+  if (num_scenes <= 0 || width <= 0 || height <= 0)
+    return set_err(nullptr, PBR_ERR_INVALID, "num_scenes, width and height must be positive (got %d, %d, %d)",
+                   num_scenes, width, height);
+  if (width > 65535 || height > 65535)
+    return set_err(nullptr, PBR_ERR_INVALID, "width and height must be at most 65535");
+  if ((long long)width * height > (1LL << 30) || (long long)num_scenes * width * height * 4 > (1LL << 62))
+    return set_err(nullptr, PBR_ERR_INVALID, "image too large");
+  if (channels < 1 || channels > 4) return set_err(nullptr, PBR_ERR_INVALID, "channels must be 1..4 (got %d)", channels);
+  if (flags != 0) return set_err(nullptr, PBR_ERR_INVALID, "flags must be 0");
+  pbr_ctx* ctx = new pbr_ctx();
+  memset(&ctx->P, 0, sizeof(ctx->P));
+  cudaError_t e = cudaGetDevice(&ctx->device);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return set_err(nullptr, PBR_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  }
+  cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
+  cudaDeviceGetAttribute(&ctx->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+  ctx->P.N = num_scenes;
+  ctx->P.W = width;
+  ctx->P.H = height;
+  ctx->P.C = channels;
+  ctx->P.cull = 1;
+  ctx->P.bg[3] = 1.f;
+  ctx->P.bg_packed = pack_bg(ctx->P.bg);
+  ctx->P.ldir[2] = 1.f;
+  ctx->P.ldir_raw[2] = 1.f;
+  ctx->P.znear = 0.05f;
+  ctx->P.zfar = 100.f;
+  ctx->P.sigma = 0.5f / (2.f * std::log(9.f));
+  ctx->P.gamma = 1e-3f;
+  ctx->P.max_tris = 1;
+  e = cudaMalloc(&ctx->d_counter, 2 * sizeof(int32_t));
+  if (e != cudaSuccess) {
+    delete ctx;
+    return set_err(nullptr, PBR_ERR_CUDA, "cudaMalloc: %s", cudaGetErrorString(e));
+  }
+  ctx->d_status = ctx->d_counter + 1;
+  e = cudaMemset(ctx->d_counter, 0, 2 * sizeof(int32_t));
+  if (e != cudaSuccess) {
+    cudaFree(ctx->d_counter);
+    delete ctx;
+    return set_err(nullptr, PBR_ERR_CUDA, "cudaMemset: %s", cudaGetErrorString(e));
+  }
+  *out_ctx = ctx;
+  return PBR_OK;
+}
+
+int pbr_destroy(pbr_ctx* ctx) {
+  if (!ctx) return PBR_OK;
+  cudaFree(ctx->d_counter);
+  cudaFree(ctx->d_zbuf);
+  cudaFree(ctx->d_cbuf);
+  delete ctx;
+  return PBR_OK;
+}
+
+int pbr_mesh_register(pbr_ctx* ctx, const float* d_pos, const float* d_nrm, const int32_t* d_idx, int nv, int nt,
+                      int smooth, int* out_mesh_id) {
+  PBR_CHECK_CTX(ctx);
+  if (!out_mesh_id) return set_err(ctx, PBR_ERR_INVALID, "out_mesh_id is null");
+  if (ctx->P.num_meshes >= pbr::kMaxMeshes)
+    return set_err(ctx, PBR_ERR_CAPACITY, "at most %d meshes per renderer", pbr::kMaxMeshes);
+  if (nv <= 0 || nt < 0) return set_err(ctx, PBR_ERR_INVALID, "mesh needs nv > 0 and nt >= 0");
+  if (!d_pos || !d_nrm || (nt > 0 && !d_idx)) return set_err(ctx, PBR_ERR_INVALID, "mesh pointers must be non-null");
+  MeshDesc& m = ctx->P.meshes[ctx->P.num_meshes];
+  m.pos = d_pos;
+  m.nrm = d_nrm;
+  m.idx = d_idx;
+  m.nv = nv;
+  m.nt = nt;
+  m.smooth = smooth ? 1 : 0;
+  ctx->P.max_tris = std::max(ctx->P.max_tris, nt);
+  *out_mesh_id = ctx->P.num_meshes++;
+  return PBR_OK;
+}
+
+int pbr_node_add(pbr_ctx* ctx, int mesh_id, int instances_per_scene, int shared, int* out_node_id) {
+  PBR_CHECK_CTX(ctx);
+  if (!out_node_id) return set_err(ctx, PBR_ERR_INVALID, "out_node_id is null");
+  if (ctx->P.num_nodes >= pbr::kMaxNodes)
+    return set_err(ctx, PBR_ERR_CAPACITY, "at most %d nodes per renderer", pbr::kMaxNodes);
+  if (mesh_id < 0 || mesh_id >= ctx->P.num_meshes) return set_err(ctx, PBR_ERR_INVALID, "unknown mesh id %d", mesh_id);
+  if (instances_per_scene < 0) return set_err(ctx, PBR_ERR_INVALID, "instances_per_scene must be >= 0");
+  const int n = ctx->P.num_nodes;
+  NodeDesc& nd = ctx->P.nodes[n];
+  memset(&nd, 0, sizeof(nd));
+  nd.mesh = mesh_id;
+  nd.ips = instances_per_scene;
+  nd.shared = shared ? 1 : 0;
+  nd.mode = pbr::kModeHpr;
+  int rank = 0;
+  for (int i = 0; i < n; ++i) rank += ctx->P.nodes[i].ips;
+  nd.rank_base = rank;
+  ctx->P.num_nodes++;
+  ctx->node_ready.push_back(false);
+  *out_node_id = n;
+  return PBR_OK;
+}
+
+int pbr_node_set_buffers(pbr_ctx* ctx, int node_id, int mode, const float* d_pos, const float* d_rot,
+                         const float* d_scale, const float* d_color, const int32_t* d_counts) {
+  PBR_CHECK_CTX(ctx);
+  if (node_id < 0 || node_id >= ctx->P.num_nodes) return set_err(ctx, PBR_ERR_INVALID, "unknown node id %d", node_id);
+  if (mode != pbr::kModeHpr && mode != pbr::kModeRot && mode != pbr::kModeMat)
+    return set_err(ctx, PBR_ERR_INVALID, "unknown rotation mode %d", mode);
+  if (!d_rot || !d_color) return set_err(ctx, PBR_ERR_INVALID, "rotation and colour buffers must be non-null");
+  if (mode != pbr::kModeMat && (!d_pos || !d_scale))
+    return set_err(ctx, PBR_ERR_INVALID, "position and scale buffers must be non-null");
+  NodeDesc& nd = ctx->P.nodes[node_id];
+  nd.mode = mode;
+  nd.pos = d_pos;
+  nd.rot = d_rot;
+  nd.scale = d_scale;
+  nd.color = d_color;
+  nd.counts = d_counts;
+  ctx->node_ready[node_id] = true;
+  return PBR_OK;
+}
+
+int pbr_camera_bind(pbr_ctx* ctx, const float* d_vp, float z_near, float z_far) {
+  PBR_CHECK_CTX(ctx);
+  if (!d_vp) return set_err(ctx, PBR_ERR_INVALID, "d_vp is null");
+  if (!(z_far > z_near)) return set_err(ctx, PBR_ERR_INVALID, "z_far must be greater than z_near");
+  ctx->P.vp = d_vp;
+  ctx->P.znear = z_near;
+  ctx->P.zfar = z_far;
+  ctx->cam_bound = true;
+  return PBR_OK;
+}
+
+int pbr_light_set(pbr_ctx* ctx, const float ambient[3], const float direction[3], const float color[3],
+                  float strength) {
+  PBR_CHECK_CTX(ctx);
+  if (!ambient || !direction || !color) return set_err(ctx, PBR_ERR_INVALID, "light arrays must be non-null");
+  const double l = std::sqrt((double)direction[0] * direction[0] + (double)direction[1] * direction[1] +
+                             (double)direction[2] * direction[2]);
+  for (int i = 0; i < 3; ++i) {
+    ctx->P.amb[i] = ambient[i];
+    ctx->P.lcol[i] = color[i];
+    ctx->P.ldir_raw[i] = direction[i];
+    ctx->P.ldir[i] = l > 0 ? (float)(direction[i] / l) : 0.f;
+  }
+  ctx->P.strength = std::min(std::max(strength, 0.f), 1.f);
+  return PBR_OK;
+}
+
+int pbr_background_set(pbr_ctx* ctx, const float rgba[4]) {
+  PBR_CHECK_CTX(ctx);
+  if (!rgba) return set_err(ctx, PBR_ERR_INVALID, "rgba is null");
+  for (int i = 0; i < 4; ++i) ctx->P.bg[i] = rgba[i];
+  ctx->P.bg_packed = pack_bg(ctx->P.bg);
+  return PBR_OK;
+}
+
+int pbr_raster_config(pbr_ctx* ctx, int threads, int bin_px, int tri_cap, int persistent) {
+  PBR_CHECK_CTX(ctx);
+  if (threads != 128 && threads != 256 && threads != 512)
+    return set_err(ctx, PBR_ERR_INVALID, "threads must be 128, 256 or 512 (got %d)", threads);
+  if (bin_px != 8 && bin_px != 16 && bin_px != 32)
+    return set_err(ctx, PBR_ERR_INVALID, "bin_px must be 8, 16 or 32 (got %d)", bin_px);
+  if (tri_cap != 0 && (tri_cap < 64 || tri_cap > 4096 || (tri_cap % 32) != 0))
+    return set_err(ctx, PBR_ERR_INVALID, "tri_cap must be 0 or a multiple of 32 in [64, 4096]");
+  ctx->threads = threads;
+  ctx->bin_px = bin_px;
+  ctx->tri_cap_req = tri_cap;
+  ctx->persistent = persistent ? 1 : 0;
+  return PBR_OK;
+}
+
+static int render_with(pbr_ctx* ctx, int threads, int bin_px, int tri_cap, int persistent, uint8_t* d_out,
+                       float* d_depth, int32_t* d_winner, cudaStream_t s) {
+  LaunchPlan lp;
+  const bool winner = d_winner != nullptr;
+  int rc = plan_launch(ctx, threads, bin_px, tri_cap, persistent, false, winner, 0, ctx->P.num_nodes, &lp);
+  if (rc) return rc;
+  lp.A.out = d_out;
+  lp.A.depth = d_depth;
+  lp.A.winner = d_winner;
+  if (persistent) {
+    cudaError_t e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMemsetAsync");
+  }
+  cudaError_t e = pbr::hard_launch(threads, false, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "hard raster launch");
+  return PBR_OK;
+}
+
+int pbr_render(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, int32_t* d_winner, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
+  int rc = check_ready(ctx, 0, ctx->P.num_nodes);
+  if (rc) return rc;
+  return render_with(ctx, ctx->threads, ctx->bin_px, ctx->tri_cap_req, ctx->persistent, d_out, d_depth, d_winner,
+                     (cudaStream_t)stream);
+}
+
+int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_threads, int* out_bin_px, int* out_tri_cap,
+                 int* out_persistent, float* out_ms) {
+  PBR_CHECK_CTX(ctx);
+  if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
+  int rc = check_ready(ctx, 0, ctx->P.num_nodes);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int thr[3] = {128, 256, 512};
+  const int bins[3] = {8, 16, 32};
+  float best = 1e30f;
+  int bt = ctx->threads, bb = ctx->bin_px, bp = ctx->persistent, bc = ctx->tri_cap_req;
+  const long long need = 2 * scene_source_tris(ctx, 0, ctx->P.num_nodes);
+  std::vector<int> caps = {0};
+  if (need > 256) { caps.push_back(256); caps.push_back(512); }
+  int status = PBR_OK;
+  for (int ti = 0; ti < 3 && status == PBR_OK; ++ti)
+    for (int bi = 0; bi < 3 && status == PBR_OK; ++bi)
+      for (int pi = 0; pi < 2 && status == PBR_OK; ++pi)
+        for (int cap : caps) {
+          // warm-up + 3 timed launches
+          int r = render_with(ctx, thr[ti], bins[bi], cap, pi, d_out, nullptr, nullptr, s);
+          if (r == PBR_ERR_CAPACITY) { ctx->err.clear(); continue; }
+          if (r) { status = r; break; }
+          cudaEventRecord(e0, s);
+          for (int rep = 0; rep < 3; ++rep) render_with(ctx, thr[ti], bins[bi], cap, pi, d_out, nullptr, nullptr, s);
+          cudaEventRecord(e1, s);
+          cudaError_t ce = cudaEventSynchronize(e1);
+          if (ce != cudaSuccess) { status = cuda_err(ctx, ce, "autotune"); break; }
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          ms /= 3.f;
+          if (ms < best) {
+            best = ms;
+            bt = thr[ti]; bb = bins[bi]; bp = pi; bc = cap;
+          }
+        }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (status) return status;
+  ctx->threads = bt;
+  ctx->bin_px = bb;
+  ctx->persistent = bp;
+  ctx->tri_cap_req = bc;
+  if (out_threads) *out_threads = bt;
+  if (out_bin_px) *out_bin_px = bb;
+  if (out_tri_cap) *out_tri_cap = bc;
+  if (out_persistent) *out_persistent = bp;
+  if (out_ms) *out_ms = best;
+  return PBR_OK;
+}
+
+static int ensure_plain_buffers(pbr_ctx* ctx) {
+  if (ctx->d_zbuf) return PBR_OK;
+  const size_t n = (size_t)ctx->P.N * ctx->P.W * ctx->P.H;
+  cudaError_t e = cudaMalloc(&ctx->d_zbuf, n * sizeof(float));
+  if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMalloc (plain depth buffer)");
+  e = cudaMalloc(&ctx->d_cbuf, n * sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    cudaFree(ctx->d_zbuf);
+    ctx->d_zbuf = nullptr;
+    return cuda_err(ctx, e, "cudaMalloc (plain colour buffer)");
+  }
+  return PBR_OK;
+}
+
+int pbr_plain_clear(pbr_ctx* ctx, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  int rc = ensure_plain_buffers(ctx);
+  if (rc) return rc;
+  cudaError_t e = pbr::plain_clear_launch(ctx->P, ctx->d_zbuf, ctx->d_cbuf, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "plain clear launch");
+  return PBR_OK;
+}
+
+int pbr_plain_draw(pbr_ctx* ctx, int node_id, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  if (node_id < 0 || node_id >= ctx->P.num_nodes) return set_err(ctx, PBR_ERR_INVALID, "unknown node id %d", node_id);
+  if (!ctx->d_zbuf) return set_err(ctx, PBR_ERR_STATE, "pbr_plain_clear must run first");
+  int rc = check_ready(ctx, node_id, node_id + 1);
+  if (rc) return rc;
+  LaunchPlan lp;
+  rc = plan_launch(ctx, 256, 16, 0, 0, true, false, node_id, node_id + 1, &lp);
+  if (rc) return rc;
+  lp.A.zbuf = ctx->d_zbuf;
+  lp.A.cbuf = ctx->d_cbuf;
+  cudaError_t e = pbr::hard_launch(256, true, false, ctx->P, lp.A, lp.grid, lp.smem, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "plain draw launch");
+  return PBR_OK;
+}
+
+int pbr_plain_resolve(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
+  if (!ctx->d_zbuf) return set_err(ctx, PBR_ERR_STATE, "pbr_plain_clear must run first");
+  cudaError_t e = pbr::plain_resolve_launch(ctx->P, ctx->d_zbuf, ctx->d_cbuf, d_out, d_depth, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "plain resolve launch");
+  return PBR_OK;
+}
+
+int pbr_debug_transforms(pbr_ctx* ctx, int node_id, float* d_out, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  if (node_id < 0 || node_id >= ctx->P.num_nodes) return set_err(ctx, PBR_ERR_INVALID, "unknown node id %d", node_id);
+  if (!ctx->node_ready[node_id]) return set_err(ctx, PBR_ERR_STATE, "node %d has no buffers bound", node_id);
+  if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
+  const NodeDesc& nd = ctx->P.nodes[node_id];
+  const long long rows = nd.shared ? (long long)nd.ips : (long long)nd.ips * ctx->P.N;
+  cudaError_t e = pbr::debug_transforms_launch(nd, rows, d_out, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "debug transforms launch");
+  return PBR_OK;
+}
+
+int pbr_device_status(pbr_ctx* ctx, int32_t* out_flags) {
+  PBR_CHECK_CTX(ctx);
+  if (!out_flags) return set_err(ctx, PBR_ERR_INVALID, "out_flags is null");
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_err(ctx, e, "cudaDeviceSynchronize");
+  int32_t v = 0;
+  e = cudaMemcpy(&v, ctx->d_status, sizeof(v), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMemcpy");
+  e = cudaMemset(ctx->d_status, 0, sizeof(int32_t));
+  if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMemset");
+  *out_flags = v;
+  return PBR_OK;
+}
+
+}  // extern "C"

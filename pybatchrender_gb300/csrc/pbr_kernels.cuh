@@ -1,0 +1,126 @@
+// pbr_kernels.cuh -- device-side scene description shared by the raster kernels
+// and the C ABI (pbr_capi.cu).
+//
+// Everything a launch needs travels by value in the kernel parameters
+// (SceneParams + RasterArgs, < 4 KB), so a launch captured into a CUDA graph
+// replays with the same buffer addresses and the caller updates the scene by
+// writing those buffers in place.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pbr {
+
+constexpr int kMaxNodes = 24;
+constexpr int kMaxMeshes = 24;
+constexpr int kPx = 16;  // pixels per thread: one 128-bit store per channel
+
+enum : int { kModeHpr = 0, kModeRot = 1, kModeMat = 2 };
+
+// Device error flags (RasterArgs::status, OR-ed).
+enum : int {
+  kStatusIdOverflow = 1,   // winner id did not fit in 31 bits
+  kStatusCapacity = 2,     // a chunk could not hold one round of triangles
+};
+
+struct MeshDesc {
+  const float* pos;    // [nv,3]
+  const float* nrm;    // [nv,3]
+  const int32_t* idx;  // [nt,3]
+  int32_t nv, nt, smooth, pad;
+};
+
+struct NodeDesc {
+  const int32_t* counts;  // [N] or null
+  const float* pos;       // [B,3]
+  const float* rot;       // [B,3] | [B,9] | [B,16]
+  const float* scale;     // [B]
+  const float* color;     // [B,4]
+  float* gpos;            // soft-mode gradients (may be null)
+  float* grot;
+  float* gcol;
+  int32_t mesh, ips, shared, mode;
+  int32_t rank_base, pad0, pad1, pad2;
+};
+
+struct SceneParams {
+  int32_t N, W, H, C;
+  const float* vp;  // [N,16] row-major
+  float amb[3];
+  float lcol[3];
+  float ldir[3];     // normalised direction towards the light
+  float ldir_raw[3]; // as given (the soft backward differentiates through the normalisation)
+  float strength;    // clamped to [0,1]
+  float bg[4];
+  uint32_t bg_packed;
+  float znear, zfar, sigma, gamma;
+  int32_t num_nodes, num_meshes, max_tris, cull;
+  MeshDesc meshes[kMaxMeshes];
+  NodeDesc nodes[kMaxNodes];
+};
+
+struct RasterArgs {
+  uint8_t* out;       // [N,C,H,W]
+  float* depth;       // [N,H,W] or null
+  int32_t* winner;    // [N,H,W] or null
+  float* zbuf;        // plain mode: [N*H*W]
+  uint32_t* cbuf;     // plain mode: [N*H*W] packed RGBA8
+  int32_t* work_counter;  // persistent scheduling
+  int32_t* status;
+  int32_t node_begin, node_end;
+  int32_t bin_px, bins_x;
+  int32_t tri_cap, vcap, icap;
+  int32_t region_px, regions_per_scene, num_items;
+  int32_t max_region_bins;
+  int32_t persistent;
+  int32_t smooth_any;
+  int32_t multi_chunk;
+};
+
+// Shared-memory carve-up, identical on host (to size the launch) and device.
+struct SmemLayout {
+  int t0, t1, t2, t3, t4;  // float4 [tri_cap]: three edges, depth plane + x-box, meta
+  int s0, s1, s2, s3;      // float4 [tri_cap]: smooth-shading attributes (if smooth_any)
+  int masks;               // uint32 [max_region_bins * tri_cap/32]
+  int vcache;              // float4 [vcap*2]: clip position, world normal
+  int icache;              // float4 [icap*4]: model matrix rows, colour
+  int state;               // per-pixel state across chunks [kPx][threads] (z, rgba, id)
+  int misc;                // scan scratch, VP, work item
+  int total;
+};
+
+__host__ __device__ inline int align16(int b) { return (b + 15) & ~15; }
+
+__host__ __device__ inline SmemLayout smem_layout(const RasterArgs& a, int threads, bool winner) {
+  SmemLayout L;
+  int off = 0;
+  const int t4 = a.tri_cap * 16;
+  L.t0 = off; off += align16(t4);
+  L.t1 = off; off += align16(t4);
+  L.t2 = off; off += align16(t4);
+  L.t3 = off; off += align16(t4);
+  L.t4 = off; off += align16(t4);
+  if (a.smooth_any) {
+    L.s0 = off; off += align16(t4);
+    L.s1 = off; off += align16(t4);
+    L.s2 = off; off += align16(t4);
+    L.s3 = off; off += align16(t4);
+  } else {
+    L.s0 = L.s1 = L.s2 = L.s3 = 0;
+  }
+  L.masks = off; off += align16(a.max_region_bins * (a.tri_cap / 32) * 4);
+  L.vcache = off; off += align16(a.vcap * 32);
+  L.icache = off; off += align16(a.icap * 64);
+  if (a.multi_chunk) {
+    L.state = off;
+    off += align16(threads * kPx * (winner ? 12 : 8));
+  } else {
+    L.state = 0;
+  }
+  L.misc = off; off += align16((threads / 32 + 8) * 4 + 16 * 4 + 16);
+  L.total = off;
+  return L;
+}
+
+}  // namespace pbr

@@ -1,0 +1,22 @@
+// pbr_launch.h -- host-side launchers exported by the .cu translation units to
+// the C ABI layer (pbr_capi.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "pbr_kernels.cuh"
+
+namespace pbr {
+
+// Hard raster (pbr_hard.cu).  threads in {128, 256, 512}; plain selects the
+// per-node variant that reads/writes the global depth/colour buffer.
+cudaError_t hard_set_smem_limit(int threads, bool plain, bool winner, int bytes);
+cudaError_t hard_occupancy(int threads, bool plain, bool winner, int smem_bytes, int* blocks_per_sm);
+cudaError_t hard_launch(int threads, bool plain, bool winner, const SceneParams& P, const RasterArgs& A,
+                        int grid, int smem_bytes, cudaStream_t stream);
+cudaError_t plain_clear_launch(const SceneParams& P, float* zbuf, uint32_t* cbuf, cudaStream_t stream);
+cudaError_t plain_resolve_launch(const SceneParams& P, const float* zbuf, const uint32_t* cbuf, uint8_t* out,
+                                 float* depth, cudaStream_t stream);
+cudaError_t debug_transforms_launch(const NodeDesc& node, long long rows, float* out, cudaStream_t stream);
+
+}  // namespace pbr

@@ -1,0 +1,208 @@
+"""``PBREnv``: TorchRL environment base over a ``PBRRenderer`` (``pybatchrender/env.py``).
+
+When TorchRL and tensordict are installed ``PBREnv`` subclasses
+``torchrl.envs.EnvBase`` and uses its specs, exactly like the reference
+(``env.py:18-95,360-440``).  Without them (neither package is part of this
+project's environments) a small stand-in with the same ``reset`` / ``step``
+contract is used: tensordicts become :class:`TensorDictLite`, a dict keyed by
+strings or nested tuples with a ``batch_size``.
+"""
+from __future__ import annotations
+
+from abc import abstractmethod
+
+import torch
+
+from .config import PBRConfig
+
+try:  # pragma: no cover - depends on the environment
+    from tensordict import TensorDict as _TensorDict
+    from torchrl.data.tensor_specs import Categorical, Composite, Unbounded
+    from torchrl.envs import EnvBase as _EnvBase
+    from torchrl.envs import ParallelEnv as _ParallelEnv
+    HAVE_TORCHRL = True
+except Exception:
+    HAVE_TORCHRL = False
+    _TensorDict = None
+    _ParallelEnv = None
+
+
+class TensorDictLite(dict):
+    """Minimal tensordict stand-in: string or nested-tuple keys, ``batch_size``."""
+
+    def __init__(self, fields=None, batch_size=None):
+        super().__init__()
+        self.batch_size = torch.Size(batch_size or [])
+        for k, v in (fields or {}).items():
+            self[k] = v
+
+    def __getitem__(self, key):
+        if isinstance(key, tuple):
+            cur = self
+            for k in key:
+                cur = dict.__getitem__(cur, k)
+            return cur
+        return dict.__getitem__(self, key)
+
+    def __setitem__(self, key, value):
+        if isinstance(key, tuple):
+            cur = self
+            for k in key[:-1]:
+                if k not in cur:
+                    dict.__setitem__(cur, k, TensorDictLite(batch_size=self.batch_size))
+                cur = dict.__getitem__(cur, k)
+            dict.__setitem__(cur, key[-1], value)
+        else:
+            dict.__setitem__(self, key, value)
+
+    def get(self, key, default=None):
+        try:
+            return self[key]
+        except KeyError:
+            return default
+
+    def keys(self, include_nested: bool = False):
+        return list(dict.keys(self))
+
+
+def TensorDict(fields, batch_size=None):  # noqa: N802 - mirrors the tensordict constructor
+    if HAVE_TORCHRL:
+        return _TensorDict(fields, batch_size=batch_size)
+    return TensorDictLite(fields, batch_size=batch_size)
+
+
+class _SpecLite:
+    def __init__(self, shape, dtype, device, n=None):
+        self.shape, self.dtype, self.device, self.n = torch.Size(shape), dtype, device, n
+
+    def rand(self):
+        if self.n is not None:
+            return torch.randint(0, self.n, self.shape, dtype=self.dtype, device=self.device)
+        return torch.randn(self.shape, dtype=self.dtype, device=self.device)
+
+    def zero(self):
+        return torch.zeros(self.shape, dtype=self.dtype, device=self.device)
+
+
+class _EnvBaseLite:
+    """The slice of ``torchrl.envs.EnvBase`` the PBR envs use."""
+
+    def __init__(self, device="cpu", batch_size=torch.Size([]), **kwargs):
+        self.device = torch.device(device)
+        self.batch_size = torch.Size(batch_size)
+
+    def reset(self, tensordict=None):
+        return self._reset(tensordict)
+
+    def step(self, tensordict):
+        nxt = self._step(tensordict)
+        tensordict["next"] = nxt
+        return tensordict
+
+    def rand_action(self, tensordict=None):
+        td = tensordict if tensordict is not None else TensorDict({}, batch_size=self.batch_size)
+        td["action"] = self.action_spec.rand()
+        return td
+
+    def set_seed(self, seed: int, static_seed: bool = False):
+        self._set_seed(seed)
+        return seed
+
+
+_Base = _EnvBase if HAVE_TORCHRL else _EnvBaseLite
+
+
+class PBREnv(_Base):
+    """Environment base: owns a renderer and renders pixels per step."""
+
+    def __init__(self, renderer, cfg: PBRConfig | None = None, device: str | torch.device = "cpu",
+                 batch_size: torch.Size = torch.Size([128]), **kwargs) -> None:
+        super().__init__(device=torch.device(device), batch_size=batch_size, **kwargs)
+        self._renderer = renderer
+        self.cfg = cfg if cfg is not None else renderer.cfg
+
+    def set_default_specs(self, *, direct_obs_dim: int | None = None, actions: int | None = None,
+                          with_pixels: bool = False, pixels_only: bool = False,
+                          discrete_actions: bool = True) -> None:
+        """Observation / action / reward / done specs (``env.py:33-82``)."""
+        assert with_pixels or not pixels_only, "Cannot set both with_pixels and pixels_only to True."
+        bs = self.batch_size if self.batch_size != torch.Size([]) else torch.Size([1])
+        C = int(self.cfg.num_channels)
+        W, H = int(self.cfg.tile_resolution[0]), int(self.cfg.tile_resolution[1])
+        if not pixels_only and direct_obs_dim is None:
+            raise ValueError("direct_obs_dim must be provided when pixels_only=False.")
+        if actions is None:
+            raise ValueError("actions must be provided.")
+        if HAVE_TORCHRL:  # pragma: no cover
+            fields = {}
+            if with_pixels:
+                fields["pixels"] = Unbounded(shape=bs + torch.Size([C, H, W]), dtype=torch.uint8, device=self.device)
+            if not pixels_only:
+                fields["observation"] = Unbounded(shape=bs + torch.Size([int(direct_obs_dim)]), dtype=torch.float32,
+                                                  device=self.device)
+            self.observation_spec = Composite(**fields, shape=bs)
+            if discrete_actions:
+                self.action_spec = Categorical(n=int(actions), shape=bs, dtype=torch.long, device=self.device)
+            else:
+                self.action_spec = Unbounded(shape=bs + torch.Size([int(actions)]), dtype=torch.float32,
+                                             device=self.device)
+            self.reward_spec = Unbounded(shape=bs + torch.Size([1]), dtype=torch.float32, device=self.device)
+            self.done_spec = Unbounded(shape=bs + torch.Size([1]), dtype=torch.bool, device=self.device)
+            return
+        self.observation_spec = {}
+        if with_pixels:
+            self.observation_spec["pixels"] = _SpecLite(bs + torch.Size([C, H, W]), torch.uint8, self.device)
+        if not pixels_only:
+            self.observation_spec["observation"] = _SpecLite(bs + torch.Size([int(direct_obs_dim)]), torch.float32,
+                                                             self.device)
+        if discrete_actions:
+            self.action_spec = _SpecLite(bs, torch.long, self.device, n=int(actions))
+        else:
+            self.action_spec = _SpecLite(bs + torch.Size([int(actions)]), torch.float32, self.device)
+        self.reward_spec = _SpecLite(bs + torch.Size([1]), torch.float32, self.device)
+        self.done_spec = _SpecLite(bs + torch.Size([1]), torch.bool, self.device)
+
+    @abstractmethod
+    def _step(self, tensordict):
+        pass
+
+    @abstractmethod
+    def _reset(self, tensordict=None):
+        pass
+
+    def render_pixels(self, obs: torch.Tensor | None = None) -> torch.Tensor:
+        """Render ``obs`` through the renderer (``env.py:92-95``)."""
+        if self._renderer is None:
+            raise RuntimeError("Renderer is not initialized. Construct env with a renderer and pass it to PBREnv.")
+        return self._renderer.step(obs)
+
+    @classmethod
+    def make_parallel_env(cls, *, config: PBRConfig, renderer_cls, num_workers: int,
+                          mp_start_method: str = "spawn", shared_memory: bool = True):
+        """TorchRL ``ParallelEnv`` of ``num_workers`` spawned replicas, each with
+        its own renderer (``env.py:360-416``).  Needs TorchRL."""
+        if not HAVE_TORCHRL:
+            raise RuntimeError("make_parallel_env needs torchrl and tensordict, which are not installed")
+        import multiprocessing as mp  # pragma: no cover
+        try:
+            mp.set_start_method(mp_start_method, force=True)
+        except RuntimeError:
+            pass
+        kwargs = [{"env_cls": cls, "renderer_cls": renderer_cls, "config": config, "worker_index": i,
+                   "num_workers": num_workers} for i in range(int(num_workers))]
+        return _ParallelEnv(int(num_workers), create_env_fn=cls._make_env_worker, shared_memory=shared_memory,
+                            mp_start_method=mp_start_method, create_env_kwargs=kwargs)
+
+    @staticmethod
+    def _make_env_worker(env_cls, renderer_cls, config: PBRConfig, worker_index: int, num_workers: int):
+        """Spawn-safe worker factory (``env.py:418-440``): seed offset by the
+        worker index."""
+        cfg = PBRConfig.from_config(config, worker_index=worker_index, num_workers=num_workers)
+        cfg.worker_index = worker_index
+        try:
+            if getattr(cfg, "seed", None) is not None:
+                cfg.seed = int(cfg.seed) + int(worker_index)
+        except Exception:
+            pass
+        renderer = renderer_cls(cfg)
+        return env_cls(renderer=renderer, cfg=cfg)

@@ -1,0 +1,415 @@
+"""Triangle meshes for the batch renderer: procedural shapes, file loaders and
+model baking.
+
+The reference loads models through Panda3D's loader (``renderer/node.py:61-71``)
+and bakes ``model_scale`` / ``model_hpr`` / the pivot into the vertices with
+``flattenStrong`` (``renderer/node.py:214-268,313-341``).  Panda3D's bundled
+``models/box`` is a unit cube spanning ``[0,1]^3`` with one quad per face; it is
+not shipped with the reference, so it is restated here procedurally (24
+vertices, 12 triangles, per-face normals, counter-clockwise outward winding).
+
+A :class:`Mesh` is plain host data (float32 positions/normals, int32 indices).
+The renderer uploads it once to device memory at ``setup_environment``.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import struct
+from collections.abc import Sequence
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Mesh:
+    """Indexed triangle mesh.
+
+    positions: ``[nv,3]`` float32, normals: ``[nv,3]`` float32 (unit length),
+    indices: ``[nt,3]`` int32, counter-clockwise when seen from the outside.
+    ``smooth`` is False when every triangle's three vertex normals are equal
+    (flat shading); the kernels use it only as a hint.
+    """
+
+    positions: np.ndarray
+    normals: np.ndarray
+    indices: np.ndarray
+    name: str = "mesh"
+    smooth: bool = field(default=False)
+
+    def __post_init__(self) -> None:
+        self.positions = np.ascontiguousarray(self.positions, dtype=np.float32).reshape(-1, 3)
+        self.normals = np.ascontiguousarray(self.normals, dtype=np.float32).reshape(-1, 3)
+        self.indices = np.ascontiguousarray(self.indices, dtype=np.int32).reshape(-1, 3)
+        if self.positions.shape != self.normals.shape:
+            raise ValueError("positions and normals must have the same shape")
+        if self.indices.size and (self.indices.min() < 0 or self.indices.max() >= len(self.positions)):
+            raise ValueError("mesh indices out of range")
+        tri_n = self.normals[self.indices]  # [nt,3,3]
+        self.smooth = bool(np.any(np.abs(tri_n - tri_n[:, :1, :]) > 1e-7))
+
+    @property
+    def num_vertices(self) -> int:
+        return int(self.positions.shape[0])
+
+    @property
+    def num_triangles(self) -> int:
+        return int(self.indices.shape[0])
+
+    def tight_bounds(self) -> tuple[np.ndarray, np.ndarray]:
+        return self.positions.min(axis=0), self.positions.max(axis=0)
+
+    def copy(self) -> "Mesh":
+        return Mesh(self.positions.copy(), self.normals.copy(), self.indices.copy(), self.name)
+
+
+# ---------------------------------------------------------------------------
+# Procedural meshes
+# ---------------------------------------------------------------------------
+
+def unit_cube() -> Mesh:
+    """Unit cube on ``[0,1]^3``: 6 faces x 4 vertices, 12 triangles, face normals."""
+    # (normal, origin corner, edge u, edge v) with u x v == normal so that
+    # (o, o+u, o+u+v) and (o, o+u+v, o+v) wind counter-clockwise seen from outside.
+    faces = [
+        ((1, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)),
+        ((-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1)),
+        ((0, 1, 0), (1, 1, 0), (-1, 0, 0), (0, 0, 1)),
+        ((0, -1, 0), (0, 0, 0), (1, 0, 0), (0, 0, 1)),
+        ((0, 0, 1), (0, 0, 1), (1, 0, 0), (0, 1, 0)),
+        ((0, 0, -1), (0, 1, 0), (1, 0, 0), (0, -1, 0)),
+    ]
+    pos, nrm, idx = [], [], []
+    for n, o, u, v in faces:
+        o, u, v = np.array(o, float), np.array(u, float), np.array(v, float)
+        assert np.allclose(np.cross(u, v), n)
+        base = len(pos)
+        for corner in (o, o + u, o + u + v, o + v):
+            pos.append(corner)
+            nrm.append(n)
+        idx += [(base, base + 1, base + 2), (base, base + 2, base + 3)]
+    return Mesh(np.array(pos), np.array(nrm), np.array(idx), name="box")
+
+
+def cylinder(segments: int = 64, radius: float = 0.5, height: float = 1.0) -> Mesh:
+    """Closed cylinder along +z centred at the origin.
+
+    Side: two rings of ``segments`` vertices with radial (smooth) normals,
+    ``2*segments`` triangles.  Caps: a centre vertex plus a ring each with flat
+    normals, ``segments`` triangles per cap.  Total ``4*segments`` triangles
+    (256 for 64 segments).
+    """
+    s = int(segments)
+    if s < 3:
+        raise ValueError("cylinder needs at least 3 segments")
+    ang = 2.0 * math.pi * np.arange(s) / s
+    ca, sa = np.cos(ang), np.sin(ang)
+    z0, z1 = -0.5 * height, 0.5 * height
+    pos, nrm, idx = [], [], []
+    # side rings
+    for z in (z0, z1):
+        for i in range(s):
+            pos.append((radius * ca[i], radius * sa[i], z))
+            nrm.append((ca[i], sa[i], 0.0))
+    for i in range(s):
+        j = (i + 1) % s
+        a0, a1, b0, b1 = i, j, s + i, s + j
+        idx += [(a0, a1, b1), (a0, b1, b0)]
+    # caps
+    for z, nz in ((z1, 1.0), (z0, -1.0)):
+        c = len(pos)
+        pos.append((0.0, 0.0, z))
+        nrm.append((0.0, 0.0, nz))
+        for i in range(s):
+            pos.append((radius * ca[i], radius * sa[i], z))
+            nrm.append((0.0, 0.0, nz))
+        for i in range(s):
+            j = (i + 1) % s
+            if nz > 0:
+                idx.append((c, c + 1 + i, c + 1 + j))
+            else:
+                idx.append((c, c + 1 + j, c + 1 + i))
+    return Mesh(np.array(pos), np.array(nrm), np.array(idx), name=f"cylinder{s}")
+
+
+def icosphere(subdivisions: int = 2, radius: float = 0.5) -> Mesh:
+    """Geodesic sphere from a subdivided icosahedron with smooth normals.
+
+    20 * 4**subdivisions triangles: 320 at level 2, 1280 at level 3.
+    """
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0),
+             (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+             (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    verts = [np.array(v, float) / np.linalg.norm(v) for v in verts]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11),
+             (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6), (7, 1, 8),
+             (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9),
+             (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    for _ in range(int(subdivisions)):
+        cache: dict[tuple[int, int], int] = {}
+
+        def mid(a: int, b: int) -> int:
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca_ = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca_), (b, bc, ab), (c, ca_, bc), (ab, bc, ca_)]
+        faces = nf
+    v = np.array(verts)
+    f = np.array(faces)
+    # make every face wind counter-clockwise seen from outside
+    p0, p1, p2 = v[f[:, 0]], v[f[:, 1]], v[f[:, 2]]
+    flip = np.einsum("ij,ij->i", np.cross(p1 - p0, p2 - p0), p0 + p1 + p2) < 0
+    f[flip] = f[flip][:, [0, 2, 1]]
+    return Mesh(v * radius, v, f, name=f"icosphere{int(subdivisions)}")
+
+
+# ---------------------------------------------------------------------------
+# File loaders (Panda3D .egg text with polygons, glTF 2.0 with an external .bin)
+# ---------------------------------------------------------------------------
+
+def _triangulate_fan(poly: Sequence[int]) -> list[tuple[int, int, int]]:
+    return [(poly[0], poly[i], poly[i + 1]) for i in range(1, len(poly) - 1)]
+
+
+def load_egg(path: str) -> Mesh:
+    """Minimal Panda3D ``.egg`` reader: one ``<VertexPool>`` of ``<Vertex>``
+    entries (position + optional ``<Normal>``) and ``<Polygon>`` entries with
+    ``<VertexRef>``.  Polygons are fan-triangulated; vertices without a normal
+    get the polygon's face normal."""
+    import re
+
+    text = open(path, "r", encoding="utf-8").read()
+    pos: dict[int, tuple[float, float, float]] = {}
+    nrm: dict[int, tuple[float, float, float]] = {}
+    for m in re.finditer(r"<Vertex>\s*(\d+)\s*\{([^{}]*(?:\{[^{}]*\}[^{}]*)*)\}", text):
+        vid = int(m.group(1))
+        body = m.group(2)
+        head = body.split("<")[0].split()
+        pos[vid] = tuple(float(x) for x in head[:3])
+        nm = re.search(r"<Normal>\s*\{([^}]*)\}", body)
+        if nm:
+            nrm[vid] = tuple(float(x) for x in nm.group(1).split()[:3])
+    polys = []
+    for m in re.finditer(r"<Polygon>\s*\{(.*?)<VertexRef>\s*\{([^}]*)\}", text, re.S):
+        refs = [int(x) for x in m.group(2).split("<")[0].split()]
+        polys.append(refs)
+    out_p, out_n, out_i = [], [], []
+    for refs in polys:
+        pts = np.array([pos[r] for r in refs], float)
+        fn = np.cross(pts[1] - pts[0], pts[2] - pts[0])
+        ln = np.linalg.norm(fn)
+        fn = fn / ln if ln > 0 else np.array([0.0, 0.0, 1.0])
+        base = len(out_p)
+        for r in refs:
+            out_p.append(pos[r])
+            out_n.append(nrm.get(r, tuple(fn)))
+        out_i += _triangulate_fan(list(range(base, base + len(refs))))
+    n = np.array(out_n, float)
+    n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-12)
+    return Mesh(np.array(out_p), n, np.array(out_i), name=os.path.basename(path))
+
+
+def load_gltf(path: str) -> Mesh:
+    """Minimal glTF 2.0 reader: first primitive of the first mesh (triangles),
+    POSITION / NORMAL float accessors and an index accessor, data in an
+    external ``.bin`` buffer."""
+    with open(path, "r", encoding="utf-8") as f:
+        doc = json.load(f)
+    base = os.path.dirname(path)
+    buffers = [open(os.path.join(base, b["uri"]), "rb").read() for b in doc["buffers"]]
+
+    def accessor(i: int) -> np.ndarray:
+        acc = doc["accessors"][i]
+        bv = doc["bufferViews"][acc["bufferView"]]
+        comp = {5126: np.float32, 5125: np.uint32, 5123: np.uint16, 5121: np.uint8}[acc["componentType"]]
+        ncomp = {"SCALAR": 1, "VEC2": 2, "VEC3": 3, "VEC4": 4}[acc["type"]]
+        off = bv.get("byteOffset", 0) + acc.get("byteOffset", 0)
+        itemsize = np.dtype(comp).itemsize * ncomp
+        stride = bv.get("byteStride", itemsize)
+        raw = buffers[bv["buffer"]]
+        if stride == itemsize:
+            arr = np.frombuffer(raw, dtype=comp, count=acc["count"] * ncomp, offset=off)
+        else:
+            arr = np.stack([np.frombuffer(raw, dtype=comp, count=ncomp, offset=off + k * stride)
+                            for k in range(acc["count"])])
+        return arr.reshape(acc["count"], ncomp)
+
+    prim = doc["meshes"][0]["primitives"][0]
+    if prim.get("mode", 4) != 4:
+        raise ValueError("only triangle-list glTF primitives are supported")
+    p = accessor(prim["attributes"]["POSITION"]).astype(np.float32)
+    if "NORMAL" in prim["attributes"]:
+        n = accessor(prim["attributes"]["NORMAL"]).astype(np.float32)
+    else:
+        n = np.zeros_like(p)
+    idx = accessor(prim["indices"]).reshape(-1, 3).astype(np.int64) if "indices" in prim else \
+        np.arange(len(p)).reshape(-1, 3)
+    if not np.any(n):
+        n = np.zeros_like(p)
+        tri = p[idx]
+        fn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+        for k in range(3):
+            np.add.at(n, idx[:, k], fn)
+    n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-12)
+    return Mesh(p, n, idx.astype(np.int32), name=os.path.basename(path))
+
+
+_BUILTIN = {
+    "box": unit_cube,
+    "cube": unit_cube,
+    "cylinder": lambda: cylinder(64),
+    "sphere": lambda: icosphere(2),
+    "icosphere": lambda: icosphere(2),
+}
+
+
+def resolve_model(model: "str | Mesh") -> Mesh:
+    """Map a reference-style model path to a mesh.
+
+    ``"models/box"`` / ``"box"`` -> :func:`unit_cube` (Panda3D's bundled box);
+    ``"cylinder"``, ``"cylinder:<segments>"``, ``"icosphere:<level>"`` ->
+    procedural shapes; an existing ``.egg`` / ``.gltf`` file -> the loaders
+    above.  A :class:`Mesh` is returned as a copy.
+    """
+    if isinstance(model, Mesh):
+        return model.copy()
+    if not isinstance(model, str):
+        raise TypeError(f"model_path must be a str or Mesh, got {type(model).__name__}")
+    if os.path.isfile(model):
+        low = model.lower()
+        if low.endswith(".egg"):
+            return load_egg(model)
+        if low.endswith(".gltf"):
+            return load_gltf(model)
+        raise ValueError(f"unsupported model file type: {model}")
+    name = model
+    if name.startswith("models/"):
+        name = name[len("models/"):]
+    for suffix in (".egg", ".bam", ".egg.pz"):
+        if name.endswith(suffix):
+            name = name[: -len(suffix)]
+    if ":" in name:
+        kind, arg = name.split(":", 1)
+        if kind == "cylinder":
+            return cylinder(int(arg))
+        if kind in ("icosphere", "sphere"):
+            return icosphere(int(arg))
+    if name in _BUILTIN:
+        return _BUILTIN[name]()
+    raise FileNotFoundError(f"unknown model '{model}' (no such file and no built-in mesh of that name)")
+
+
+# ---------------------------------------------------------------------------
+# Baking (Panda3D setScale / setHpr / flattenStrong / pivot_to_rel)
+# ---------------------------------------------------------------------------
+
+def panda_hpr_matrix(h_deg: float, p_deg: float, r_deg: float) -> np.ndarray:
+    """Rotation of Panda3D's ``NodePath.setHpr`` (degrees) for column vectors:
+    roll about +y, then pitch about +x, then heading about +z
+    (``R = Rz(h) @ Rx(p) @ Ry(r)``).  Only ``model_hpr`` baking uses it; the
+    per-instance rotations use the shader convention of
+    ``renderer/shader_context.py:47-84`` instead."""
+    h, p, r = (math.radians(float(a)) for a in (h_deg, p_deg, r_deg))
+    ch, sh, cp, sp, cr, sr = math.cos(h), math.sin(h), math.cos(p), math.sin(p), math.cos(r), math.sin(r)
+    rz = np.array([[ch, -sh, 0], [sh, ch, 0], [0, 0, 1]])
+    rx = np.array([[1, 0, 0], [0, cp, -sp], [0, sp, cp]])
+    ry = np.array([[cr, 0, sr], [0, 1, 0], [-sr, 0, cr]])
+    return rz @ rx @ ry
+
+
+def _coerce_scale(model_scale) -> tuple[tuple[float, float, float], bool] | None:
+    """Follows ``PBRNode._coerce_model_scale`` (``renderer/node.py:180-201``)."""
+    if model_scale is None:
+        return None
+    if isinstance(model_scale, (int, float)):
+        v = float(model_scale)
+        return (v, v, v), True
+    if isinstance(model_scale, Sequence) or isinstance(model_scale, np.ndarray):
+        seq = tuple(float(v) for v in model_scale)
+        if len(seq) == 0:
+            raise ValueError("model_scale sequence cannot be empty")
+        if len(seq) == 1:
+            return (seq[0],) * 3, True
+        if len(seq) != 3:
+            raise ValueError("model_scale sequence must have length 1 or 3")
+        return seq, False
+    raise TypeError("model_scale must be a number, a sequence of length 1 or 3, or None")
+
+
+def _coerce_hpr(model_hpr) -> tuple[float, float, float] | None:
+    """Follows ``PBRNode._coerce_model_hpr`` (``renderer/node.py:203-212``)."""
+    if model_hpr is None:
+        return None
+    if not (isinstance(model_hpr, Sequence) or isinstance(model_hpr, np.ndarray)):
+        raise TypeError("model_hpr must be a sequence of length 3 or None")
+    hpr = tuple(float(v) for v in model_hpr)
+    if len(hpr) != 3:
+        raise ValueError("model_hpr sequence must have length 3")
+    return hpr
+
+
+def bake(mesh: Mesh, model_scale=None, model_hpr=None, pivot_relative_point=None,
+         model_scale_units: str = "relative") -> Mesh:
+    """Bake model scale, model HPR and pivot into the vertices.
+
+    Mirrors ``renderer/node.py:61-67``: ``_apply_model_scale`` (``:214-260``;
+    "absolute" divides the target size by the tight-bounds extent, uniform
+    targets by the longest side), ``_apply_model_hpr`` (``:262-268``), the
+    ``flattenStrong`` bake, then ``pivot_to_rel`` (``:313-341``) which moves the
+    bounds-relative point to the origin.  Normals are transformed by the
+    inverse transpose and renormalised, as Panda3D's flatten does.
+    """
+    out = mesh.copy()
+    p = out.positions.astype(np.float64)
+    n = out.normals.astype(np.float64)
+    lin = np.eye(3)
+    coerced = _coerce_scale(model_scale)
+    if coerced is not None:
+        vals, uniform = coerced
+        if model_scale_units == "relative":
+            svec = np.array(vals)
+        elif model_scale_units == "absolute":
+            lo, hi = p.min(axis=0), p.max(axis=0)
+            dims = hi - lo
+            longest = max(float(dims.max()), 1e-8)
+            if uniform:
+                svec = np.full(3, vals[0] / longest)
+            else:
+                comps = []
+                for target, src in zip(vals, dims):
+                    denom = src if abs(src) >= 1e-8 else longest
+                    if abs(denom) < 1e-8:
+                        denom = 1.0
+                    comps.append(target / denom)
+                svec = np.array(comps)
+        else:
+            raise ValueError(f"Unknown model_scale_units '{model_scale_units}'")
+        lin = np.diag(svec) @ lin
+    hpr = _coerce_hpr(model_hpr)
+    if hpr is not None:
+        lin = panda_hpr_matrix(*hpr) @ lin
+    p = p @ lin.T
+    if coerced is not None or hpr is not None:
+        det = np.linalg.det(lin)
+        if abs(det) > 0:
+            n = n @ np.linalg.inv(lin)
+            n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-12)
+        if det < 0:  # mirrored transform: keep counter-clockwise outward winding
+            out.indices = out.indices[:, [0, 2, 1]].copy()
+    if pivot_relative_point is not None:
+        lo, hi = p.min(axis=0), p.max(axis=0)
+        rel = np.array([float(v) for v in pivot_relative_point])
+        p = p - (lo + (hi - lo) * rel)
+    out.positions = p.astype(np.float32)
+    out.normals = n.astype(np.float32)
+    return Mesh(out.positions, out.normals, out.indices, mesh.name)

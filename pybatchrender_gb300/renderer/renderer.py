@@ -1,0 +1,422 @@
+"""``PBRRenderer``: the reference's renderer API (``renderer/renderer.py``)
+on top of the sm_103a kernels in ``libpbr.so``.
+
+The reference subclasses Panda3D's ShowBase, draws one instanced GL call per
+node into a ``cols x rows`` atlas and reads it back into ``[N,C,H,W]``
+(``renderer.py:326-363``).  Here the scene state is device tensors, and
+``step()`` runs the subclass hook ``_step`` then one kernel launch that writes
+the final ``[N,C,H,W]`` uint8 pixels.  Two raster methods:
+
+* ``raster_method='batched'`` (default): one fused launch for all nodes,
+  matrices built on the device, optionally captured with ``_step`` into a
+  CUDA graph (``cuda_graph=True``).
+* ``raster_method='plain'``: the reference's per-step flow -- per node, host
+  (CPU torch) matrix building, a host-to-device copy and one launch into a
+  depth/colour buffer, then a resolve launch and a synchronisation.
+
+There is no CPU fallback: on a machine without a CUDA device the scene API
+works (it is plain tensor bookkeeping) but rendering raises
+:class:`RendererUnavailable`.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from collections.abc import Sequence
+from typing import Literal
+
+import numpy as np
+import torch
+
+from .. import _capi
+from .._capi import RendererUnavailable
+from ..config import PBRConfig
+from .camera import PBRCam
+from .light import PBRLight
+from .node import MODE_MAT, PBRNode, mesh_key
+
+
+class PBRRenderer:
+    """Batch renderer for ``num_scenes`` independent scenes."""
+
+    def __init__(self, cfg: PBRConfig | dict | None = None, **cfg_overrides):
+        self.cfg = PBRConfig.from_config(cfg, **cfg_overrides)
+        self.num_scenes = int(self.cfg.num_scenes)
+        self.device = torch.device(self.cfg.device)
+        if self.device.type == "cuda" and self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        # the plain method keeps per-instance state on the host like the reference
+        self.state_device = torch.device("cpu") if self.cfg.raster_method == "plain" else self.device
+        self._pbr_nodes: list[PBRNode] = []
+        self._pbr_cam: PBRCam | None = None
+        self._pbr_light: PBRLight | None = None
+        self._background_color = (0.0, 0.0, 0.0, 1.0)
+        self._fps_text = None
+        self._ctx = None
+        self._lib = None
+        self._unavailable: str | None = None
+        self._graph = None
+        self._static_out = None
+        self._static_depth = None
+        self._plain_staging: dict = {}
+        self.autotune_result = None
+
+    # ------------------------------------------------------------- scene API
+    def set_background_color(self, r: float, g: float, b: float, a: float = 1.0) -> None:
+        self._background_color = (float(r), float(g), float(b), float(a))
+        if self._ctx is not None:
+            _capi.call(self._lib, self._ctx, "pbr_background_set", (ctypes.c_float * 4)(*self._background_color))
+            self._graph = None
+
+    def add_node(self,
+                 model_path,
+                 instances_per_scene: int,
+                 texture=None,
+                 model_pivot_relative_point: tuple[float, float, float] | None = None,
+                 model_scale: float | Sequence[float] | None = None,
+                 model_hpr: tuple[float, float, float] | None = None,
+                 model_scale_units: Literal["relative", "absolute"] = "relative",
+                 positions: "torch.Tensor | None" = None,
+                 hprs: "torch.Tensor | None" = None,
+                 scales: "torch.Tensor | None" = None,
+                 colors: "torch.Tensor | None" = None,
+                 backend: Literal["loop", "instanced"] = "instanced",
+                 shared_across_scenes: bool = False,
+                 parent: "PBRNode | None" = None,
+                 name: str | None = None) -> PBRNode:
+        node = PBRNode(self, model_path=model_path, num_scenes=self.num_scenes,
+                       instances_per_scene=int(instances_per_scene), texture=texture,
+                       model_pivot_relative_point=model_pivot_relative_point, model_scale=model_scale,
+                       model_hpr=model_hpr, model_scale_units=model_scale_units, positions=positions,
+                       hprs=hprs, scales=scales, colors=colors, backend=backend,
+                       shared_across_scenes=shared_across_scenes, parent=parent, name=name)
+        if self._ctx is not None:
+            self._build_context()
+        return node
+
+    def add_camera(self, fov_y_deg: float = 55.0, z_near: float = 0.05, z_far: float = 100.0,
+                   fixed_projection: bool = True) -> PBRCam:
+        self._pbr_cam = PBRCam(self, num_scenes=self.cfg.num_scenes, cols=self.cfg.tiles[0], rows=self.cfg.tiles[1],
+                               fov_y_deg=fov_y_deg, z_near=z_near, z_far=z_far, fixed_projection=fixed_projection)
+        if self._ctx is not None:
+            self._camera_changed(self._pbr_cam)
+        return self._pbr_cam
+
+    def _set_tiles_auto(self) -> None:
+        if self._pbr_cam is None:
+            self.add_camera()
+        self._pbr_cam._set_tiles()
+
+    def add_light(self, ambient: tuple[float, float, float] = (0.2, 0.2, 0.25),
+                  dir_dir: tuple[float, float, float] = (0.4, -0.6, -0.7),
+                  dir_col: tuple[float, float, float] = (1.0, 1.0, 1.0),
+                  strength: float = 1.0) -> PBRLight:
+        self._pbr_light = PBRLight(self, ambient=ambient, dir_dir=dir_dir, dir_col=dir_col, strength=strength)
+        return self._pbr_light
+
+    def setup_environment(self) -> None:
+        """Finish scene construction (``renderer.py:400-406``): add a default
+        camera if none, create the CUDA context, bind every buffer and, with
+        ``cfg.autotune``, pick the fastest launch configuration."""
+        if self._pbr_cam is None:
+            self.add_camera()
+        if self.device.type != "cuda":
+            self._unavailable = f"the renderer needs a CUDA device (cfg.device={self.cfg.device!r})"
+            return
+        self._build_context()
+        if self.cfg.autotune and self.cfg.raster_method == "batched" and self.cfg.raster_mode == "hard":
+            self.autotune()
+
+    # ---------------------------------------------------------------- stepping
+    def _step(self, *args, **kwargs):
+        """Subclass hook: write the scene state for this step (default no-op)."""
+        return None
+
+    def _interactive_step(self):
+        return None
+
+    def step(self, *args, return_pixels: bool = True, **kwargs):
+        """Run ``_step(*args, **kwargs)`` then render; returns uint8
+        ``[N,C,H,W]`` on the CUDA device (plus float32 ``[N,H,W]`` depth when
+        ``cfg.return_depth``), ``None`` when ``return_pixels`` is False
+        (``renderer.py:377-390``)."""
+        if self.cfg.cuda_graph and return_pixels and not self.cfg.interactive \
+                and self.cfg.raster_method == "batched" and self.cfg.raster_mode == "hard":
+            return self._graph_step(args, kwargs)
+        if not getattr(self.cfg, "interactive", False):
+            self._step(*args, **kwargs)
+        if return_pixels:
+            return self.render()
+        return None
+
+    def __call__(self, *args, return_pixels: bool = True, **kwargs):
+        return self.step(*args, return_pixels=return_pixels, **kwargs)
+
+    # --------------------------------------------------------------- rendering
+    def _require_ready(self) -> None:
+        if self._ctx is None:
+            if self._unavailable:
+                raise RendererUnavailable(self._unavailable)
+            raise RuntimeError("setup_environment() must be called before rendering")
+
+    def _stream(self) -> int:
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _out_shape(self) -> tuple[int, int, int, int]:
+        W, H = self.cfg.tile_resolution
+        return (self.num_scenes, int(self.cfg.num_channels), int(H), int(W))
+
+    def render(self, return_depth: bool | None = None, return_winner: bool = False):
+        """Render the current scene state (no ``_step``)."""
+        self._require_ready()
+        want_depth = self.cfg.return_depth if return_depth is None else bool(return_depth)
+        if self.cfg.raster_method == "plain":
+            out, depth = self._render_plain(want_depth)
+            return (out, depth) if want_depth else out
+        N, C, H, W = self._out_shape()
+        if self.cfg.reuse_output:
+            if self._static_out is None:
+                self._static_out = torch.empty((N, C, H, W), dtype=torch.uint8, device=self.device)
+            out = self._static_out
+            if want_depth and self._static_depth is None:
+                self._static_depth = torch.empty((N, H, W), dtype=torch.float32, device=self.device)
+            depth = self._static_depth if want_depth else None
+        else:
+            out = torch.empty((N, C, H, W), dtype=torch.uint8, device=self.device)
+            depth = torch.empty((N, H, W), dtype=torch.float32, device=self.device) if want_depth else None
+        winner = torch.empty((N, H, W), dtype=torch.int32, device=self.device) if return_winner else None
+        _capi.call(self._lib, self._ctx, "pbr_render", _capi.ptr(out), _capi.ptr(depth), _capi.ptr(winner),
+                   self._stream())
+        res = [out]
+        if want_depth:
+            res.append(depth)
+        if return_winner:
+            res.append(winner)
+        return res[0] if len(res) == 1 else tuple(res)
+
+    def _render_plain(self, want_depth: bool):
+        """The reference's per-step flow on the GPU: per node, host matrices
+        (``node.py:116-126``) -> host-to-device copy -> one draw launch; then
+        a resolve launch and a blocking synchronisation (the readback of
+        ``renderer.py:326-350``)."""
+        N, C, H, W = self._out_shape()
+        stream = self._stream()
+        out = torch.empty((N, C, H, W), dtype=torch.uint8, device=self.device)
+        depth = torch.empty((N, H, W), dtype=torch.float32, device=self.device) if want_depth else None
+        _capi.call(self._lib, self._ctx, "pbr_plain_clear", stream)
+        for node, nid in self._node_ids.items():
+            mats_d, col_d = self._plain_staging[nid]
+            mats_d.copy_(node.get_transforms().reshape(-1, 16))
+            col_d.copy_(node.color)
+            _capi.call(self._lib, self._ctx, "pbr_plain_draw", nid, stream)
+        _capi.call(self._lib, self._ctx, "pbr_plain_resolve", _capi.ptr(out), _capi.ptr(depth), stream)
+        torch.cuda.synchronize(self.device)
+        return out, depth
+
+    def _graph_step(self, args, kwargs):
+        sig = tuple((tuple(a.shape), a.dtype) if torch.is_tensor(a) else ("v", a) for a in args)
+        if self._graph is None or self._graph_sig != sig:
+            self._graph = None
+            static = [a.detach().to(self.device).clone() if torch.is_tensor(a) else a for a in args]
+            N, C, H, W = self._out_shape()
+            self._static_out = torch.empty((N, C, H, W), dtype=torch.uint8, device=self.device)
+            self._static_depth = torch.empty((N, H, W), dtype=torch.float32, device=self.device) \
+                if self.cfg.return_depth else None
+            side = torch.cuda.Stream(self.device)
+            side.wait_stream(torch.cuda.current_stream(self.device))
+            with torch.cuda.stream(side):
+                for _ in range(2):
+                    self._step(*static, **kwargs)
+                    self._launch_static()
+            torch.cuda.current_stream(self.device).wait_stream(side)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._step(*static, **kwargs)
+                self._launch_static()
+            self._graph, self._graph_sig, self._graph_static = g, sig, static
+        else:
+            for dst, src in zip(self._graph_static, args):
+                if torch.is_tensor(dst):
+                    dst.copy_(src, non_blocking=True)
+        self._graph.replay()
+        return (self._static_out, self._static_depth) if self.cfg.return_depth else self._static_out
+
+    def _launch_static(self) -> None:
+        _capi.call(self._lib, self._ctx, "pbr_render", _capi.ptr(self._static_out), _capi.ptr(self._static_depth),
+                   None, self._stream())
+
+    def autotune(self) -> dict:
+        """Time the launch configurations (threads, bin size, chunk size,
+        persistent schedule) on the current scene and keep the fastest."""
+        self._require_ready()
+        N, C, H, W = self._out_shape()
+        scratch = torch.empty((N, C, H, W), dtype=torch.uint8, device=self.device)
+        vals = [ctypes.c_int() for _ in range(4)]
+        ms = ctypes.c_float()
+        _capi.call(self._lib, self._ctx, "pbr_autotune", _capi.ptr(scratch), self._stream(),
+                   *[ctypes.byref(v) for v in vals], ctypes.byref(ms))
+        self.autotune_result = {"threads": vals[0].value, "bin_px": vals[1].value, "tri_cap": vals[2].value,
+                                "persistent": vals[3].value, "ms": ms.value}
+        self._graph = None
+        return self.autotune_result
+
+    def debug_transforms(self, node: PBRNode) -> torch.Tensor:
+        """(B,4,4) model matrices as the kernels build them (for tests)."""
+        self._require_ready()
+        nid = self._node_ids[node]
+        out = torch.empty((node.buf_instances, 16), dtype=torch.float32, device=self.device)
+        _capi.call(self._lib, self._ctx, "pbr_debug_transforms", nid, _capi.ptr(out), self._stream())
+        return out.reshape(-1, 4, 4)
+
+    # ----------------------------------------------------------- atlas views
+    def to_atlas(self, pixels: torch.Tensor) -> torch.Tensor:
+        """Arrange ``[N,C,H,W]`` images into the reference's atlas
+        ``[rows*H, cols*W, C]`` (row 0 at the top): the inverse of
+        ``_rearrange_img``."""
+        cols, rows = self.cfg.tiles
+        N, C, H, W = pixels.shape
+        full = torch.zeros((rows * cols, C, H, W), dtype=pixels.dtype, device=pixels.device)
+        full[:N] = pixels
+        return full.view(rows, cols, C, H, W).permute(0, 3, 1, 4, 2).reshape(rows * H, cols * W, C)
+
+    def grab_pixels(self) -> torch.Tensor:
+        """Atlas image of the current state, ``[H_win, W_win, C]`` uint8."""
+        return self.to_atlas(self.render(return_depth=False))
+
+    def _rearrange_img(self, img: torch.Tensor) -> torch.Tensor:
+        """Atlas ``[H_win, W_win, C]`` -> ``[N,C,H,W]`` (``renderer.py:352-363``)."""
+        img = img.permute(2, 0, 1)
+        img = img.reshape(self.cfg.num_channels, self.cfg.tiles[1], self.cfg.tile_resolution[1],
+                          self.cfg.tiles[0], self.cfg.tile_resolution[0])
+        img = img.permute(1, 3, 0, 2, 4)
+        img = img.reshape(-1, self.cfg.num_channels, self.cfg.tile_resolution[1], self.cfg.tile_resolution[0])
+        return img[:self.cfg.num_scenes]
+
+    # ------------------------------------------------------------ export
+    def geometry_nodes(self) -> list[PBRNode]:
+        return [n for n in self._pbr_nodes if n.has_geometry and n.instances_per_scene > 0]
+
+    def export_scene(self) -> tuple[dict, list, list]:
+        """Host copy of the whole scene in the oracle's format:
+        ``(scene, meshes, nodes)``."""
+        if self._pbr_cam is None:
+            self.add_camera()
+        cam = self._pbr_cam
+        W, H = self.cfg.tile_resolution
+        light = self._pbr_light
+        scene = {
+            "N": self.num_scenes, "W": int(W), "H": int(H), "C": int(self.cfg.num_channels),
+            "vp": cam.VP_k44.detach().cpu().numpy().reshape(-1, 16),
+            "ambient": light.ambient if light else (0.0, 0.0, 0.0),
+            "ldir": light.dir_dir if light else (0.0, 0.0, 1.0),
+            "lcol": light.dir_col if light else (0.0, 0.0, 0.0),
+            "strength": min(max(light.strength, 0.0), 1.0) if light else 0.0,
+            "bg": self._background_color, "cull": 1,
+            "znear": cam.z_near, "zfar": cam.z_far,
+            "sigma": self.cfg.soft_sigma, "gamma": self.cfg.soft_gamma,
+        }
+        meshes, keys, nodes = [], {}, []
+        for node in self.geometry_nodes():
+            key = mesh_key(node.mesh)
+            if key not in keys:
+                keys[key] = len(meshes)
+                meshes.append(node.mesh)
+            d = node.export()
+            d["mesh"] = keys[key]
+            nodes.append(d)
+        return scene, meshes, nodes
+
+    # -------------------------------------------------------- context plumbing
+    def _build_context(self) -> None:
+        self.close()
+        lib = _capi.load()
+        ctx = ctypes.c_void_p()
+        W, H = self.cfg.tile_resolution
+        with torch.cuda.device(self.device):
+            rc = lib.pbr_create(ctypes.byref(ctx), self.num_scenes, int(W), int(H), int(self.cfg.num_channels), 0)
+            if rc != 0:
+                raise _capi.PBRError("pbr_create", rc, lib.pbr_last_error(None).decode())
+            self._lib, self._ctx = lib, ctx
+            self._mesh_tensors = []
+            self._node_ids: dict[PBRNode, int] = {}
+            mesh_ids: dict[bytes, int] = {}
+            for node in self.geometry_nodes():
+                key = mesh_key(node.mesh)
+                if key not in mesh_ids:
+                    m = node.mesh
+                    pos = torch.from_numpy(m.positions).to(self.device)
+                    nrm = torch.from_numpy(m.normals).to(self.device)
+                    idx = torch.from_numpy(m.indices).to(self.device)
+                    self._mesh_tensors.append((pos, nrm, idx))
+                    mid = ctypes.c_int()
+                    _capi.call(lib, ctx, "pbr_mesh_register", _capi.ptr(pos), _capi.ptr(nrm), _capi.ptr(idx),
+                               m.num_vertices, m.num_triangles, int(m.smooth), ctypes.byref(mid))
+                    mesh_ids[key] = mid.value
+                nid = ctypes.c_int()
+                _capi.call(lib, ctx, "pbr_node_add", mesh_ids[key], node.instances_per_scene,
+                           int(node.shared_across), ctypes.byref(nid))
+                self._node_ids[node] = nid.value
+                self._bind_node_buffers(node)
+            self._camera_changed(self._pbr_cam)
+            self._light_changed(self._pbr_light)
+            _capi.call(lib, ctx, "pbr_background_set", (ctypes.c_float * 4)(*self._background_color))
+            _capi.call(lib, ctx, "pbr_raster_config", int(self.cfg.raster_threads), int(self.cfg.bin_size),
+                       int(self.cfg.tri_cap), int(bool(self.cfg.persistent)))
+
+    def _bind_node_buffers(self, node: PBRNode) -> None:
+        nid = self._node_ids[node]
+        counts = node.counts
+        if counts is not None and counts.device != self.device:
+            counts = counts.to(self.device)
+            self._counts_dev = getattr(self, "_counts_dev", {})
+            self._counts_dev[nid] = counts
+        if self.cfg.raster_method == "plain":
+            mats = torch.empty((node.buf_instances, 16), dtype=torch.float32, device=self.device)
+            col = torch.empty((node.buf_instances, 4), dtype=torch.float32, device=self.device)
+            self._plain_staging[nid] = (mats, col)
+            _capi.call(self._lib, self._ctx, "pbr_node_set_buffers", nid, MODE_MAT, None, _capi.ptr(mats), None,
+                       _capi.ptr(col), _capi.ptr(counts))
+            return
+        mode, pos, rot, scale, color = node.kernel_buffers()
+        _capi.call(self._lib, self._ctx, "pbr_node_set_buffers", nid, mode, _capi.ptr(pos), _capi.ptr(rot),
+                   _capi.ptr(scale), _capi.ptr(color), _capi.ptr(counts))
+
+    def _rebind_node(self, node: PBRNode) -> None:
+        if self._ctx is not None and node in getattr(self, "_node_ids", {}):
+            self._bind_node_buffers(node)
+            self._graph = None
+
+    def _camera_changed(self, cam: PBRCam) -> None:
+        if self._ctx is not None and cam is not None:
+            _capi.call(self._lib, self._ctx, "pbr_camera_bind", _capi.ptr(cam.VP_k44), float(cam.z_near),
+                       float(cam.z_far))
+            self._graph = None
+
+    def _light_changed(self, light: PBRLight | None) -> None:
+        if self._ctx is None:
+            return
+        f3 = ctypes.c_float * 3
+        if light is None:
+            _capi.call(self._lib, self._ctx, "pbr_light_set", f3(0, 0, 0), f3(0, 0, 1), f3(0, 0, 0), 0.0)
+        else:
+            _capi.call(self._lib, self._ctx, "pbr_light_set", f3(*light.ambient), f3(*light.dir_dir),
+                       f3(*light.dir_col), float(light.strength))
+        self._graph = None
+
+    def close(self) -> None:
+        if self._ctx is not None:
+            if torch.cuda.is_available():
+                torch.cuda.synchronize(self.device)
+            self._lib.pbr_destroy(self._ctx)
+            self._ctx = None
+            self._graph = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # reference compatibility (Panda3D task manager / FPS report)
+    def report_fps(self, task=None):
+        return None

@@ -1,0 +1,58 @@
+"""The C ABI library loads and exports every entry point include/pbr_capi.h
+declares (no compute calls: runs without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from pybatchrender_gb300 import _capi
+from pybatchrender_gb300.build import LIB_PATH, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions() -> list[str]:
+    names = []
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names += re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(pbr_[a-z_0-9]+)\s*\(", text, flags=re.M)
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build()
+    return ctypes.CDLL(LIB_PATH)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "pbr_render" in names and "pbr_create" in names and len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"missing exports: {missing}"
+
+
+def test_python_binding_covers_every_symbol():
+    names = set(declared_functions()) - {"pbr_last_error"}
+    assert names <= set(_capi.SIGNATURES), sorted(names - set(_capi.SIGNATURES))
+
+
+def test_version_and_error_paths_without_gpu(lib):
+    lib.pbr_version.restype = ctypes.c_int
+    assert lib.pbr_version() >= 100
+    lib.pbr_last_error.restype = ctypes.c_char_p
+    lib.pbr_last_error.argtypes = [ctypes.c_void_p]
+    ctx = ctypes.c_void_p()
+    # invalid arguments are rejected before any CUDA call
+    rc = lib.pbr_create(ctypes.byref(ctx), 0, 64, 64, 3, 0)
+    assert rc == _capi.PBR_ERR_INVALID
+    assert b"positive" in lib.pbr_last_error(None)
+    rc = lib.pbr_create(ctypes.byref(ctx), 4, 64, 64, 7, 0)
+    assert rc == _capi.PBR_ERR_INVALID
+    assert lib.pbr_render(None, None, None, None, None) == _capi.PBR_ERR_INVALID

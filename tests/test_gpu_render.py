@@ -1,0 +1,209 @@
+"""Hard-raster parity: the CUDA renderer (through the C ABI) against the FP64
+oracle (oracle/raster_ref.c) on the same seeded scenes.
+
+Bar (the benchmark spec): winner (which triangle covers the pixel, i.e. coverage and
+depth order) identical to the oracle except at pixels the oracle flags as
+ambiguous (centre within 1e-4 px of an edge of a visible triangle, or two
+fragments within 2e-6 in window depth); colour within 1/255 per channel on
+>= 99.5 % of all pixels and on every unambiguous pixel; window depth within
+1e-5 on unambiguous covered pixels.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import pybatchrender_gb300 as pbr
+from pybatchrender_gb300 import workloads
+from pybatchrender_gb300.envs.cartpole import CartPoleConfig, CartPoleRenderer
+
+pytestmark = pytest.mark.gpu
+
+
+def check_parity(r, oracle, *, depth_tol=1e-5, min_within_1=0.995, **render_kw):
+    pix, depth, win = r.render(return_depth=True, return_winner=True, **render_kw)
+    torch.cuda.synchronize()
+    sc, me, no = r.export_scene()
+    ref = oracle.render_hard(sc, me, no, want_depth=True, want_winner=True, want_ambiguous=True)
+    gpu = {"pixels": pix.cpu().numpy(), "winner": win.cpu().numpy(), "depth": depth.cpu().numpy()}
+    cmp = oracle.compare_hard(gpu, ref)
+    assert cmp["winner_mismatch"] == 0, cmp
+    assert cmp["color_max_diff_unambiguous"] <= 1, cmp
+    assert cmp["color_within_1"] >= min_within_1, cmp
+    covered = (ref["winner"] >= 0) & ~ref["ambiguous"]
+    if covered.any():
+        assert np.abs(gpu["depth"] - ref["depth"])[covered].max() <= depth_tol, cmp
+    bg = (ref["winner"] < 0) & ~ref["ambiguous"]
+    assert np.all(gpu["depth"][bg] == 1.0)
+    return cmp, gpu, ref
+
+
+def test_cartpole_bench_256_parity(cuda, oracle):
+    r = workloads.cartpole_bench(num_scenes=256, res=64, seed=1)
+    r._step(workloads.cartpole_states(256, seed=2, device=cuda))
+    cmp, gpu, ref = check_parity(r, oracle)
+    assert (ref["winner"] >= 0).mean() > 0.01  # the scene is not empty
+    assert cmp["ambiguous"] < 0.01 * cmp["pixels"]
+
+
+def test_reference_cartpole_scene_parity(cuda, oracle):
+    """The reference's own CartPole scene (shared rail, cart, pole)."""
+    r = CartPoleRenderer(CartPoleConfig(num_scenes=64))
+    g = torch.Generator().manual_seed(3)
+    st = torch.zeros((64, 4))
+    st[:, 0] = torch.rand(64, generator=g) * 4 - 2
+    st[:, 2] = torch.rand(64, generator=g) - 0.5
+    r._step(st.to(cuda))
+    check_parity(r, oracle)
+
+
+def test_many_cubes_parity(cuda, oracle):
+    r = workloads.many_cubes(num_scenes=16, res=128, instances=64, seed=4)
+    check_parity(r, oracle)
+
+
+@pytest.mark.parametrize("tri_cap", [0, 64])
+def test_uneven_mixed_meshes_parity(cuda, oracle, tri_cap):
+    """Smooth meshes (perspective-correct normals), per-scene counts, and with
+    tri_cap=64 the multi-chunk path."""
+    r = workloads.uneven(num_scenes=24, res=84, max_instances=24, seed=5, tri_cap=tri_cap)
+    check_parity(r, oracle)
+
+
+def test_plain_matches_batched(cuda, oracle):
+    st = workloads.cartpole_states(64, seed=7, device=cuda)
+    a = workloads.cartpole_bench(num_scenes=64, seed=6)
+    b = workloads.cartpole_bench(num_scenes=64, seed=6, raster_method="plain")
+    a._step(st)
+    b._step(st.cpu())
+    pa, da = a.render(return_depth=True)
+    pb, db = b.render(return_depth=True)
+    assert torch.equal(pa, pb)
+    assert torch.equal(da, db)
+
+
+@pytest.mark.parametrize("threads", [128, 256, 512])
+@pytest.mark.parametrize("bin_px", [8, 16, 32])
+@pytest.mark.parametrize("persistent", [False, True])
+def test_launch_configs_bitwise_equal(cuda, threads, bin_px, persistent):
+    r = workloads.many_cubes(num_scenes=8, res=96, instances=32, seed=8)
+    ref = r.render().clone()
+    r.cfg.raster_threads, r.cfg.bin_size, r.cfg.persistent = threads, bin_px, persistent
+    r._build_context()
+    assert torch.equal(r.render(), ref)
+
+
+def test_deterministic_and_graph_replay(cuda):
+    r = workloads.cartpole_bench(num_scenes=128, seed=9, cuda_graph=True)
+    st1 = workloads.cartpole_states(128, seed=10, device=cuda)
+    st2 = workloads.cartpole_states(128, seed=11, device=cuda)
+    e = workloads.cartpole_bench(num_scenes=128, seed=9)
+    e._step(st1)
+    ref1 = e.render().clone()
+    e._step(st2)
+    ref2 = e.render().clone()
+    out1 = r.step(st1).clone()
+    out2 = r.step(st2).clone()
+    out1b = r.step(st1).clone()
+    assert torch.equal(out1, ref1) and torch.equal(out2, ref2) and torch.equal(out1b, ref1)
+    assert not torch.equal(ref1, ref2)
+
+
+def test_autotune_keeps_output(cuda):
+    r = workloads.many_cubes(num_scenes=8, res=64, instances=16, seed=12)
+    before = r.render().clone()
+    res = r.autotune()
+    assert res["threads"] in (128, 256, 512) and res["bin_px"] in (8, 16, 32) and res["ms"] > 0
+    assert torch.equal(r.render(), before)
+
+
+def test_debug_transforms_match_oracle(cuda, oracle):
+    r = workloads.many_cubes(num_scenes=4, res=32, instances=8, seed=13)
+    node = r.cubes
+    got = r.debug_transforms(node).cpu().numpy()
+    want = oracle.instance_matrices(dict(node.export(), mesh=0))
+    assert np.allclose(got, want, rtol=1e-5, atol=1e-5)
+    # set_transforms keeps the reference's rotation / scale / translation split
+    M = torch.tensor(want.copy())
+    M[:, 0:3, 0:3] *= 1.5
+    node.set_transforms(M)
+    got2 = r.debug_transforms(node).cpu().numpy()
+    assert np.allclose(got2, M.numpy(), rtol=1e-5, atol=1e-5)
+    assert node.mode == 1
+
+
+@pytest.mark.parametrize("channels", [1, 4])
+def test_channel_counts(cuda, oracle, channels):
+    r = workloads.cartpole_bench(num_scenes=16, seed=14, num_channels=channels)
+    r.set_background_color(0.1, 0.2, 0.3, 0.5)
+    r._step(workloads.cartpole_states(16, seed=15, device=cuda))
+    cmp, gpu, ref = check_parity(r, oracle)
+    assert gpu["pixels"].shape[1] == channels
+
+
+def test_small_and_odd_images(cuda, oracle):
+    for res in [(12, 10), (33, 17), (84, 84)]:
+        r = pbr.PBRRenderer(num_scenes=5, tile_resolution=res)
+        node = r.add_node("icosphere:2", 3, model_pivot_relative_point=(0.5, 0.5, 0.5))
+        g = torch.Generator().manual_seed(16)
+        node.set_positions(torch.rand((15, 3), generator=g) * 4 - 2)
+        node.set_scales(torch.rand(15, generator=g) * 2 + 1)
+        node.set_colors(torch.rand((15, 4), generator=g))
+        r.add_camera(fov_y_deg=50)
+        r._pbr_cam.set_positions_and_lookat([0.0, -9.0, 2.0], [0.0, 0.0, 0.0])
+        r.add_light()
+        r.setup_environment()
+        check_parity(r, oracle)
+
+
+def test_near_plane_clipping(cuda, oracle):
+    """Camera inside a large cube and cubes crossing the near plane."""
+    r = pbr.PBRRenderer(num_scenes=3, tile_resolution=(64, 64))
+    big = r.add_node("models/box", 1, model_pivot_relative_point=(0.5, 0.5, 0.5), model_scale=6.0)
+    small = r.add_node("models/box", 4, model_pivot_relative_point=(0.5, 0.5, 0.5))
+    big.set_colors(torch.tensor([0.3, 0.6, 0.9, 1.0]))
+    small.set_positions(torch.tensor([[0.0, 0.05, 0.0], [0.5, 1.0, 0.2], [-0.3, 2.0, -0.2], [0.0, -0.2, 0.5]]).repeat(3, 1))
+    small.set_hprs(torch.rand((12, 3), generator=torch.Generator().manual_seed(17)) * 6)
+    r.add_camera()
+    r._pbr_cam.set_positions_and_lookat(torch.tensor([[0.0, -0.4, 0.0], [0.2, -0.5, 0.1], [0.0, 0.0, 0.0]]),
+                                        torch.tensor([[0.0, 5.0, 0.0], [0.0, 5.0, 1.0], [1.0, 5.0, 0.0]]))
+    r.add_light()
+    # two-sided: the big cube is seen from inside, so its back faces are culled like GL does
+    r.setup_environment()
+    cmp, gpu, ref = check_parity(r, oracle)
+
+
+def test_empty_and_degenerate_inputs(cuda, oracle):
+    # no nodes at all: background everywhere
+    r = pbr.PBRRenderer(num_scenes=2, tile_resolution=(32, 32))
+    r.set_background_color(0.25, 0.5, 0.75)
+    r.setup_environment()
+    out = r.render()
+    assert torch.all(out[:, 0] == 64) and torch.all(out[:, 1] == 128) and torch.all(out[:, 2] == 191)
+    # NaN / inf poses and zero scale draw nothing and do not fault
+    r = pbr.PBRRenderer(num_scenes=4, tile_resolution=(32, 32))
+    n = r.add_node("models/box", 2)
+    pos = torch.zeros((8, 3))
+    pos[0, 0] = float("nan")
+    pos[1, 1] = float("inf")
+    n.set_positions(pos)
+    sc = torch.ones(8)
+    sc[2] = 0.0
+    n.set_scales(sc)
+    r.add_camera()
+    r.setup_environment()
+    check_parity(r, oracle)
+    # zero active instances
+    n.set_active_counts(torch.zeros(4, dtype=torch.int32))
+    assert torch.all(r.render() == 0)
+
+
+def test_env_step_renders(cuda):
+    env = pbr.envs.make("CartPole-v0", num_scenes=32)
+    td = env.reset()
+    assert td["pixels"].shape == (32, 3, 64, 64) and td["pixels"].dtype == torch.uint8
+    td["action"] = env.action_spec.rand()
+    td = env.step(td)
+    assert td["next", "pixels"].shape == (32, 3, 64, 64)
+    assert td["next", "pixels"].float().mean() > 0

@@ -1,0 +1,388 @@
+"""Benchmark: frames/s of PBRRenderer.step(return_pixels=True) on one GB300.
+
+Workload (headline): CartPole render, 4096 scenes x 64x64 RGB uint8, two unit
+cubes per scene (the benchmark CartPole scene of pybatchrender_gb300.workloads),
+seeded synthetic states.  A step = write the step's states into the scene
+(``_step``) + one render of all scenes.  One frame = one scene image
+(steps x scenes / s, as the reference's cartpole benchmark counts).
+
+Reported variants (all on the same scene and states):
+  value        batched renderer, whole step captured in a CUDA graph, inputs
+               resident in HBM; per-step CUDA-event time with the L2 flushed
+               (a 256 MiB write) before every step, flush excluded.
+  e2e          the same call through the public API with host buffers:
+               states copied from pinned host memory and pixels copied back to
+               pinned host memory inside the timed region (wall clock).
+  variants     plain per-launch path (host-built matrices, a host-to-device
+               copy per node, one launch per node, a synchronise), batched
+               eager (no graph), batched graph; soft_fwd (differentiable
+               soft-coverage forward, float32) and fwd_bwd (soft forward +
+               adjoint kernel with a constant dL/dout) on the same scene.
+  roofline     the hard-raster kernel alone: algorithmic bytes per launch /
+               mean CUDA-event duration, against the measured HBM copy peak.
+  cpu_baseline the oracle's FP32 rasteriser (a CPU port of the reference's
+               shader path) on all host threads, bounded sample.
+
+--impl reference runs that CPU port as the reference arm (the reference's own
+render path is Panda3D + OpenGL, which cannot run without a graphics stack).
+Under torchrun every rank renders its own 4096 scenes (independent replicas,
+weak scaling); value = all frames / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+METRIC = "frames/s, 4096 scenes @64x64: plain vs batched graph vs fwd+bwd; %HBM peak"
+UNIT = "frames/s"
+BYTES_PER_INSTANCE = 80  # 4x4 f32 matrix or pose + RGBA f32 colour
+BYTES_PER_SCENE = 80     # VP 4x4 f32 + light/tile
+
+
+def algorithmic_bytes_per_frame(C: int, H: int, W: int, inst: int) -> int:
+    return C * H * W + inst * BYTES_PER_INSTANCE + BYTES_PER_SCENE
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, copy burst)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """Per-launch DRAM bytes of `kernel` on `workload` from the committed ncu
+    summary (profiles/traffic.txt: 'kernel workload bytes'), or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 3 and not line.startswith("#") and parts[0] == kernel and parts[1] == workload:
+            return float(parts[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the GPU works."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{index}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return None
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                rows.append((float(p[1]), float(p[2]), float(p[3]) if p[3] not in ("[N/A]", "") else 0.0, p[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        load = [r for r in rows if r[2] > 0] or rows
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in load:
+            for n, v in zip(names, r[3]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def l2_flusher(device):
+    buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+
+    def flush():
+        buf.fill_(1.0)
+    return flush
+
+
+def time_steps(fn, steps: int, flush, stream) -> list[float]:
+    """Per-step CUDA-event times (ms) on `stream`, L2 flushed before each step."""
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        flush()
+        evs[i][0].record(stream)
+        fn(i)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def cpu_port_fps(num_scenes: int, res: int, seed: int, budget_s: float, threads: int, steps: int | None = None):
+    """Frames/s of the oracle's FP32 rasteriser on `threads` host threads."""
+    from oracle import oracle
+    from pybatchrender_gb300 import workloads
+
+    oracle.build()
+    r = workloads.cartpole_bench(num_scenes=num_scenes, res=res, seed=seed, device="cpu")
+    frames, elapsed, n = 0, 0.0, 0
+    while True:
+        r._step(workloads.cartpole_states(num_scenes, seed=1000 + n))
+        sc, me, no = r.export_scene()
+        t0 = time.perf_counter()
+        oracle.render_hard(sc, me, no, precision="f32", nthreads=threads)
+        elapsed += time.perf_counter() - t0
+        frames += num_scenes
+        n += 1
+        if (steps is not None and n >= steps) or (steps is None and elapsed >= budget_s):
+            break
+    return frames / elapsed, n, elapsed
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def reduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for w in range(args.warmup):
+        cpu_port_fps(args.scenes, args.res, 0, 0.0, threads, steps=1)
+    fps, n, elapsed = cpu_port_fps(args.scenes, args.res, 0, 0.0, threads, steps=args.steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": fps, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / n,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"cartpole_bench {args.scenes} scenes {args.res}x{args.res} RGB u8",
+                   "parallelism": "cpu threads"},
+        "cpu_baseline": {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} full steps of {args.scenes} scenes (oracle FP32 rasteriser, "
+                                   "a CPU port of the reference's basic.vert/basic.frag path)"},
+        "e2e": {"value": fps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference renders through Panda3D/OpenGL, unavailable on this box (no graphics stack)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    from pybatchrender_gb300 import _capi, workloads
+
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    _capi.load(build_if_missing=True)
+    N, res = args.scenes, args.res
+    stream = torch.cuda.current_stream(device)
+    flush = l2_flusher(device)
+    states = [workloads.cartpole_states(N, seed=100 + i, device=device) for i in range(16)]
+
+    graph_r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", cuda_graph=True)
+    tuned = graph_r.autotune() if args.autotune else None
+    eager_r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", reuse_output=True)
+    if tuned:
+        eager_r.cfg.raster_kernel = tuned["kernel"]
+        eager_r.cfg.raster_threads, eager_r.cfg.bin_size = tuned["threads"], tuned["bin_px"]
+        eager_r.cfg.persistent, eager_r.cfg.tri_cap = bool(tuned["persistent"]), tuned["tri_cap"]
+        eager_r._build_context()
+    plain_r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", raster_method="plain")
+    states_cpu = [s.cpu() for s in states]
+
+    with ClockSampler(local) as clocks:
+        # warm-up (graph capture happens on the first step)
+        for i in range(max(3, args.warmup)):
+            graph_r.step(states[i % 16])
+            eager_r.step(states[i % 16])
+        torch.cuda.synchronize()
+
+        # headline: graph-captured batched step, inputs resident in HBM
+        barrier(world)
+        t = time_steps(lambda i: graph_r.step(states[i % 16]), args.steps, flush, stream)
+        barrier(world)
+        graph_ms = reduce_max(sum(t), world)
+        ms_per_step = graph_ms / args.steps
+        value = world * N * args.steps / (graph_ms / 1000.0)
+
+        # batched, no graph
+        t = time_steps(lambda i: eager_r.step(states[i % 16]), args.steps, flush, stream)
+        eager_fps = N * args.steps / (reduce_max(sum(t), world) / 1000.0)
+
+        # plain per-launch path (wall clock: it synchronises every step)
+        plain_steps = max(3, min(args.steps, args.plain_steps))
+        for i in range(2):
+            plain_r.step(states_cpu[i % 16])
+        barrier(world)
+        t0 = time.perf_counter()
+        for i in range(plain_steps):
+            plain_r.step(states_cpu[i % 16])
+        torch.cuda.synchronize()
+        plain_fps = N * plain_steps / reduce_max(time.perf_counter() - t0, world)
+
+        # the hard-raster kernel alone (roofline)
+        kt = time_steps(lambda i: eager_r.render(), args.steps, flush, stream)
+        kernel_ms = statistics.mean(kt)
+
+        # differentiable soft mode on the same scene: forward, and forward + adjoint
+        soft_r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", raster_mode="soft")
+        gout = torch.full((N, 3, res, res), 1.0 / (N * 3 * res * res), device=device)
+        soft_steps = max(3, min(args.steps, args.soft_steps))
+
+        def soft_fwd(i):
+            soft_r._step(states[i % 16])
+            soft_r._soft_forward(None)
+
+        def soft_fwd_bwd(i):
+            soft_r._step(states[i % 16])
+            out, st = soft_r._soft_forward(None)
+            soft_r._soft_backward(out, st, gout)
+        for i in range(2):
+            soft_fwd_bwd(i)
+        t = time_steps(soft_fwd, soft_steps, flush, stream)
+        soft_fwd_fps = N * soft_steps / (reduce_max(sum(t), world) / 1000.0)
+        t = time_steps(soft_fwd_bwd, soft_steps, flush, stream)
+        fwd_bwd_fps = N * soft_steps / (reduce_max(sum(t), world) / 1000.0)
+
+        # end to end through the public API with host buffers
+        host_in = [s.pin_memory() for s in states_cpu]
+        host_out = torch.empty((N, 3, res, res), dtype=torch.uint8).pin_memory()
+        dev_in = torch.empty((N, 4), dtype=torch.float32, device=device)
+        for i in range(3):
+            dev_in.copy_(host_in[i % 16], non_blocking=True)
+            host_out.copy_(graph_r.step(dev_in), non_blocking=True)
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            dev_in.copy_(host_in[i % 16], non_blocking=True)
+            pix = graph_r.step(dev_in)
+            host_out.copy_(pix, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_s = reduce_max(time.perf_counter() - t0, world)
+        e2e_fps = world * N * args.steps / e2e_s
+    clk = clocks.summary()
+
+    if rank != 0:
+        return
+    hbm_peak, peak_src = measured_peak()
+    bpf = algorithmic_bytes_per_frame(3, res, res, 2)
+    achieved = bpf * N / (kernel_ms / 1000.0) / 1e9
+    workload_name = f"cartpole{N}x{res}"
+    kname = "small_kernel" if eager_r.cfg.raster_kernel in ("warp", "auto") else "hard_kernel"
+    traffic = ncu_traffic(kname, workload_name)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"cartpole_bench {N} scenes {res}x{res} RGB u8, 2 unit cubes/scene, seeded states",
+                   "global_batch": N * world, "parallelism": f"replicas x{world}",
+                   "l2": "flushed (256 MiB write) before every timed step, flush excluded",
+                   "launch": tuned or {"kernel": graph_r.cfg.raster_kernel, "threads": graph_r.cfg.raster_threads,
+                                       "bin_px": graph_r.cfg.bin_size}},
+        "variants": {"batched_graph": value / world, "batched_eager": eager_fps, "plain": plain_fps,
+                     "graph_over_plain": (value / world) / plain_fps,
+                     "soft_fwd": soft_fwd_fps, "fwd_bwd": fwd_bwd_fps, "soft_fwd_over_fwd_bwd": soft_fwd_fps / fwd_bwd_fps},
+        "e2e": {"value": e2e_fps, "unit": UNIT, "h2d_bytes_per_step": int(N * 4 * 4),
+                "d2h_bytes_per_step": int(N * 3 * res * res)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic, "kernel": kname,
+                     "kernel_ms": kernel_ms, "bytes_per_launch": bpf * N, "peak_source": peak_src},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+    if args.cpu_baseline and world == 1:
+        threads = os.cpu_count() or 1
+        fps, n, elapsed = cpu_port_fps(N, res, 0, args.cpu_budget, threads)
+        line["cpu_baseline"] = {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{n} full steps of {N} scenes in {elapsed:.1f}s (oracle FP32 rasteriser)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scenes", type=int, default=4096)
+    ap.add_argument("--res", type=int, default=64)
+    ap.add_argument("--plain-steps", type=int, default=50)
+    ap.add_argument("--soft-steps", type=int, default=100)
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--cpu-budget", type=float, default=10.0)
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    try:
+        if args.impl == "reference":
+            run_reference(args, world, rank)
+        else:
+            run_ours(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

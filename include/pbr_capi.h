@@ -108,24 +108,28 @@ int pbr_light_set(pbr_ctx* ctx, const float ambient[3], const float direction[3]
 /* Clear colour (renderer/renderer.py:91-94,262); default (0,0,0,1). */
 int pbr_background_set(pbr_ctx* ctx, const float rgba[4]);
 
-/* Raster launch configuration: threads per CTA (128, 256 or 512), bin size in
- * pixels (8, 16 or 32), triangle capacity per chunk (0 = automatic) and
- * persistent work-stealing scheduling (0/1).  No counterpart in the
- * reference (the GL driver schedules its own work). */
-int pbr_raster_config(pbr_ctx* ctx, int threads, int bin_px, int tri_cap, int persistent);
+/* Raster launch configuration.  kernel: 0 = automatic, 1 = scene-per-warp
+ * (scenes of at most 64 source triangles, width a multiple of 16),
+ * 2 = tile kernel (one CTA per scene region, any scene size).  threads per
+ * CTA (128, 256 or 512), bin size of the tile kernel in pixels (8, 16 or 32),
+ * its triangle capacity per chunk (0 = automatic) and persistent
+ * work-stealing scheduling (0/1).  No counterpart in the reference (the GL
+ * driver schedules its own work). */
+int pbr_raster_config(pbr_ctx* ctx, int kernel, int threads, int bin_px, int tri_cap, int persistent);
 
 /* Time the candidate launch configurations on the bound scene and keep the
  * fastest.  d_out is an [N,C,H,W] uint8 scratch image.  Synchronises the
  * stream; do not call during graph capture.  Reports the choice through the
  * out pointers (any may be NULL).  No counterpart in the reference. */
-int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_threads, int* out_bin_px,
-                 int* out_tri_cap, int* out_persistent, float* out_ms);
+int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_kernel, int* out_threads,
+                 int* out_bin_px, int* out_tri_cap, int* out_persistent, float* out_ms);
 
 /* Render every scene (hard raster): d_out [N,C,H,W] uint8, optional
  * d_depth [N,H,W] float32 window depth (1.0 where nothing is drawn) and
  * optional d_winner [N,H,W] int32 (instance rank within the scene, counted
  * in node order, times the largest mesh's triangle count plus the triangle
- * index; -1 for background).  Replaces taskMgr.step() + grab_pixels +
+ * index; -1 for background).  All three must be 16-byte aligned.
+ * Replaces taskMgr.step() + grab_pixels +
  * _rearrange_img (renderer/renderer.py:377-390,326-363). */
 int pbr_render(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, int32_t* d_winner, void* stream);
 
@@ -136,6 +140,35 @@ int pbr_render(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, int32_t* d_winner, 
 int pbr_plain_clear(pbr_ctx* ctx, void* stream);
 int pbr_plain_draw(pbr_ctx* ctx, int node_id, void* stream);
 int pbr_plain_resolve(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, void* stream);
+
+/* ---- Differentiable soft-coverage mode (no counterpart in the reference) ----
+ * Per pixel p and front-facing triangle j: soft coverage
+ * D_j = prod_k sigmoid(dist_k(p) / sigma) over the three edge lines (0 beyond
+ * 16 sigma outside), normalised linear depth zs_j = (zfar - w)/(zfar - znear),
+ * shaded colour C_j (shaders/basic.frag:33-38, unclamped);
+ * out = A * softmax_j(zs_j / gamma weighted by D_j) . C + (1 - A) * bg with
+ * A = 1 - prod_j (1 - D_j).  Triangles not fully in front of the near plane
+ * are dropped.  Defaults: sigma = 0.5 / (2 ln 9) px (0.5 px 10-90 % edge),
+ * gamma = 1e-3; threads per CTA 256. */
+int pbr_soft_config(pbr_ctx* ctx, float sigma, float gamma, int threads);
+
+/* Gradient buffers of a node (float32, B rows, accumulated with +=; any may be
+ * NULL): d_gpos [B,3], d_ghpr [B,3], d_gscale [B], d_gcol [B,4] (alpha gets 0). */
+int pbr_node_set_grads(pbr_ctx* ctx, int node_id, float* d_gpos, float* d_ghpr, float* d_gscale, float* d_gcol);
+
+/* Soft forward: d_out [N,3,H,W] float32; d_stats [N,H,W,2] float32 (optional,
+ * needed by the backward): per-pixel log-sum-exp of the depth weights and a
+ * code for prod(1 - D). */
+int pbr_render_soft(pbr_ctx* ctx, float* d_out, float* d_stats, void* stream);
+
+/* Soft adjoint: given the forward's d_out and d_stats and dL/dout
+ * d_grad_out [N,3,H,W], accumulate per-instance gradients into the buffers of
+ * pbr_node_set_grads and dL/d(normalised light direction) into
+ * d_grad_light [3] (optional).  Every node must be in PBR_MODE_HPR.  Fragment
+ * lists are recomputed from the triangle setup, nothing per fragment is
+ * stored.  Uses float atomics: the summation order is not fixed. */
+int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, const float* d_grad_out,
+                      float* d_grad_light, void* stream);
 
 /* Model matrices the kernels build for one node: d_out [B,16] row-major.
  * For tests; replaces reading back matbuf (renderer/node.py:110-126). */

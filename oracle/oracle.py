@@ -81,7 +81,7 @@ def lib() -> ctypes.CDLL:
             g = getattr(_lib, f"orc_render_soft_{prec}")
             g.restype = ctypes.c_int
             g.argtypes = [ctypes.POINTER(OrcScene), ctypes.c_int, ctypes.POINTER(OrcMesh), ctypes.c_int,
-                          ctypes.POINTER(OrcNode), ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+                          ctypes.POINTER(OrcNode), ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
             h = getattr(_lib, f"orc_instance_matrices_{prec}")
             h.restype = ctypes.c_int
             h.argtypes = [ctypes.POINTER(OrcNode), ctypes.c_int64, ctypes.c_void_p]
@@ -175,14 +175,16 @@ def render_hard(scene: dict, meshes: list, nodes: list, k0: int = 0, k1: int | N
 
 
 def render_soft(scene: dict, meshes: list, nodes: list, k0: int = 0, k1: int | None = None, *,
-                precision: str = "f64") -> np.ndarray:
-    """Soft-coverage render of scenes [k0, k1) -> float32 [n,3,H,W]."""
+                precision: str = "f64", out_dtype=np.float32) -> np.ndarray:
+    """Soft-coverage render of scenes [k0, k1) -> [n,3,H,W] (float32, or
+    float64 with ``out_dtype=np.float64`` for finite differences)."""
     pk = _Packed(scene, meshes, nodes)
     N, W, H = pk.scene.N, pk.scene.W, pk.scene.H
     k1 = N if k1 is None else k1
-    out = np.zeros((N, 3, H, W), np.float32)
+    out = np.zeros((N, 3, H, W), out_dtype)
     fn = getattr(lib(), f"orc_render_soft_{precision}")
-    rc = fn(ctypes.byref(pk.scene), pk.nmeshes, pk.meshes, pk.nnodes, pk.nodes, k0, k1, _ptr(out))
+    rc = fn(ctypes.byref(pk.scene), pk.nmeshes, pk.meshes, pk.nnodes, pk.nodes, k0, k1, _ptr(out),
+            int(out.dtype == np.float64))
     if rc != 0:
         raise RuntimeError(f"oracle soft raster failed with status {rc}")
     return out[k0:k1]

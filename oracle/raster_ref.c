@@ -56,6 +56,9 @@
 
 typedef REAL real;
 
+#define SOFT_CUTOFF 16.0  /* soft coverage is 0 beyond 16 sigma outside an edge */
+#define SOFT_TAPER 4.0    /* tapered to 0 over the last 4 sigma */
+
 #define ORC_MODE_HPR 0
 #define ORC_MODE_ROT 1
 #define ORC_MODE_MAT 2
@@ -87,7 +90,7 @@ typedef struct {
     int32_t cull;           /* 1: cull back faces (default) */
     /* soft mode */
     float znear, zfar, sigma, gamma;
-    int32_t soft_dense;     /* 1: no coverage cutoff (every triangle reaches every pixel) */
+    int32_t soft_dense;     /* unused (kept for layout) */
 } orc_scene;
 
 /* ------------------------------------------------------------------------ */
@@ -192,8 +195,10 @@ static void setup_edges(stri* t) {
     }
 }
 
-/* Screen-space setup of one clipped triangle.  Returns 0 when it is culled. */
-static int setup_tri(const orc_scene* sc, const cvert* v0, const cvert* v1, const cvert* v2, stri* t) {
+/* Screen-space setup of one clipped triangle.  Returns 0 when it is culled.
+ * margin: extra pixels around the image that still count (the soft mode's
+ * coverage reaches pixels up to its cutoff distance outside the triangle). */
+static int setup_tri(const orc_scene* sc, const cvert* v0, const cvert* v1, const cvert* v2, stri* t, real margin) {
     const cvert* v[3] = {v0, v1, v2};
     for (int k = 0; k < 3; ++k) {
         real iw = (real)1 / v[k]->w;
@@ -228,8 +233,8 @@ static int setup_tri(const orc_scene* sc, const cvert* v0, const cvert* v1, cons
         if (t->sy[k] > mxy) mxy = t->sy[k];
     }
     /* pixels whose centre (x+0.5) can lie in [mn, mx], widened by one pixel */
-    real fx0 = floor(mnx - (real)0.5) - 1, fx1 = ceil(mxx - (real)0.5) + 1;
-    real fy0 = floor(mny - (real)0.5) - 1, fy1 = ceil(mxy - (real)0.5) + 1;
+    real fx0 = floor(mnx - (real)0.5 - margin) - 1, fx1 = ceil(mxx - (real)0.5 + margin) + 1;
+    real fy0 = floor(mny - (real)0.5 - margin) - 1, fy1 = ceil(mxy - (real)0.5 + margin) + 1;
     if (fx1 < 0 || fy1 < 0 || fx0 > sc->W - 1 || fy0 > sc->H - 1) return 0;
     t->x0 = fx0 < 0 ? 0 : (int)fx0;
     t->y0 = fy0 < 0 ? 0 : (int)fy0;
@@ -327,7 +332,8 @@ static void walk_scene(const orc_scene* sc, int nmeshes, const orc_mesh* meshes,
                 }
                 for (int f = 1; f + 1 < np; ++f) {
                     stri st;
-                    if (!setup_tri(sc, &poly[0], &poly[f], &poly[f + 1], &st)) continue;
+                    real margin = soft ? (real)SOFT_CUTOFF * (real)sc->sigma + 1 : 0;
+                    if (!setup_tri(sc, &poly[0], &poly[f], &poly[f + 1], &st, margin)) continue;
                     cb(user, &st, xf.c, wid_base + t);
                 }
             }
@@ -517,8 +523,10 @@ int FN(orc_instance_matrices)(const orc_node* nd, int64_t B, float* out) {
 /*
  * Per fragment (pixel p, front-facing triangle j fully in front of the near plane):
  *   e_k   = E_k(p) / |(A_k, B_k)|              signed distance to edge line k (px)
- *   D_j   = prod_k sigmoid(e_k / sigma)        soft coverage; 0 when min_k e_k < -16 sigma
- *                                              (unless soft_dense)
+ *   D_j   = prod_k sigmoid(e_k / sigma) * T(d)   soft coverage; d = Euclidean distance
+ *           from p to the triangle (0 inside), T(d) = S((16 sigma - d) / (4 sigma)),
+ *           S(x) = x^3 (6x^2 - 15x + 10) on [0,1], 0 below, 1 above: exactly 0 once
+ *           p is 16 sigma or more away from the triangle
  *   1/w   = sum_k b_k / w_k                    b_k = E_k / area2 (unclamped)
  *   zs_j  = (zfar - w) / (zfar - znear)        normalised linear depth, nearer = larger
  *   C_j   = basic.frag shading with the perspective-correct (extrapolated) normal,
@@ -527,6 +535,26 @@ int FN(orc_instance_matrices)(const orc_node* nd, int64_t B, float* out) {
  *   A     = 1 - prod_j (1 - D_j)
  *   out   = A * sum_j w_j C_j / sum_j w_j + (1 - A) * bg.rgb
  */
+
+/* smootherstep taper of the coverage tail, as a function of the distance d
+ * from the pixel to the triangle */
+static inline real soft_taper(real d, real sig) {
+    real x = ((real)SOFT_CUTOFF * sig - d) / ((real)SOFT_TAPER * sig);
+    if (x <= 0) return 0;
+    if (x >= 1) return 1;
+    return x * x * x * (x * (x * 6 - 15) + 10);
+}
+
+/* distance from (px,py) to the segment (ax,ay)-(bx,by) */
+static inline real seg_dist(real px, real py, real ax, real ay, real bx, real by) {
+    real ux = bx - ax, uy = by - ay, wx = px - ax, wy = py - ay;
+    real l2 = ux * ux + uy * uy;
+    real t = l2 > 0 ? (wx * ux + wy * uy) / l2 : 0;
+    if (t < 0) t = 0;
+    if (t > 1) t = 1;
+    real dx = px - (ax + t * ux), dy = py - (ay + t * uy);
+    return sqrt(dx * dx + dy * dy);
+}
 
 typedef struct {
     const orc_scene* sc;
@@ -537,7 +565,7 @@ typedef struct {
     real* Pi;     /* prod (1 - D)    [P] */
 } soft_ctx;
 
-#define SOFT_CUTOFF 16.0
+
 
 static void soft_cb(void* user, const stri* t, const real col[4], int32_t wid) {
     (void)wid;
@@ -547,9 +575,7 @@ static void soft_cb(void* user, const stri* t, const real col[4], int32_t wid) {
     real L[3];
     for (int k = 0; k < 3; ++k) L[k] = sqrt(t->A[k] * t->A[k] + t->B[k] * t->B[k]);
     int x0, x1, y0, y1;
-    if (sc->soft_dense) {
-        x0 = 0; y0 = 0; x1 = sc->W - 1; y1 = sc->H - 1;
-    } else {
+    {
         /* bbox widened by the cutoff distance */
         real mnx = t->sx[0], mxx = t->sx[0], mny = t->sy[0], mxy = t->sy[0];
         for (int k = 1; k < 3; ++k) {
@@ -576,9 +602,19 @@ static void soft_cb(void* user, const stri* t, const real col[4], int32_t wid) {
                 e[k] = E[k] / L[k];
                 if (e[k] < emin) emin = e[k];
             }
-            if (!sc->soft_dense && emin < -SOFT_CUTOFF * sig) continue;
-            real D = 1;
+            if (emin <= -SOFT_CUTOFF * sig) continue;
+            real dout = 0;
+            if (emin < 0) {
+                dout = 1e30;
+                for (int k = 0; k < 3; ++k) {
+                    int a = (k + 1) % 3, b = (k + 2) % 3;
+                    real d = seg_dist(px, py, t->sx[a], t->sy[a], t->sx[b], t->sy[b]);
+                    if (d < dout) dout = d;
+                }
+            }
+            real D = soft_taper(dout, sig);
             for (int k = 0; k < 3; ++k) D *= (real)1 / (1 + exp(-e[k] / sig));
+            if (!(D > 0)) continue;
             real b0 = E[0] / t->area2, b1 = E[1] / t->area2, b2 = E[2] / t->area2;
             real q0 = b0 * t->iw[0], q1 = b1 * t->iw[1], q2 = b2 * t->iw[2];
             real qs = q0 + q1 + q2;
@@ -604,9 +640,10 @@ static void soft_cb(void* user, const stri* t, const real col[4], int32_t wid) {
     }
 }
 
-/* Soft render of scenes [k0,k1) into out[N,3,H,W] (float). */
+/* Soft render of scenes [k0,k1) into out[N,3,H,W]: float, or double when
+ * out_double != 0 (finite-difference checks need the unrounded image). */
 int FN(orc_render_soft)(const orc_scene* sc, int nmeshes, const orc_mesh* meshes, int nnodes,
-                        const orc_node* nodes, int k0, int k1, float* out) {
+                        const orc_node* nodes, int k0, int k1, void* out, int out_double) {
     if (!sc || !out || k0 < 0 || k1 > sc->N || k0 > k1) return -2;
     int64_t P = (int64_t)sc->W * sc->H;
     soft_ctx s;
@@ -627,11 +664,13 @@ int FN(orc_render_soft)(const orc_scene* sc, int nmeshes, const orc_mesh* meshes
         }
         walk_scene(sc, nmeshes, meshes, nnodes, nodes, k, 1, soft_cb, &s);
         for (int c = 0; c < 3; ++c) {
-            float* dst = out + ((int64_t)k * 3 + c) * P;
             for (int64_t o = 0; o < P; ++o) {
                 real A = 1 - s.Pi[o];
                 real fg = s.S[o] > 0 ? s.acc[o * 3 + c] / s.S[o] : 0;
-                dst[o] = (float)(A * fg + (1 - A) * (real)sc->bg[c]);
+                real v = A * fg + (1 - A) * (real)sc->bg[c];
+                int64_t idx = ((int64_t)k * 3 + c) * P + o;
+                if (out_double) ((double*)out)[idx] = (double)v;
+                else ((float*)out)[idx] = (float)v;
             }
         }
     }

@@ -39,12 +39,16 @@ SIGNATURES: dict[str, list] = {
     "pbr_camera_bind": [_vp, _vp, _f, _f],
     "pbr_light_set": [_vp, _f3, _f3, _f3, _f],
     "pbr_background_set": [_vp, _f4],
-    "pbr_raster_config": [_vp, _i, _i, _i, _i],
-    "pbr_autotune": [_vp, _vp, _vp, _pi, _pi, _pi, _pi, _pf],
+    "pbr_raster_config": [_vp, _i, _i, _i, _i, _i],
+    "pbr_autotune": [_vp, _vp, _vp, _pi, _pi, _pi, _pi, _pi, _pf],
     "pbr_render": [_vp, _vp, _vp, _vp, _vp],
     "pbr_plain_clear": [_vp, _vp],
     "pbr_plain_draw": [_vp, _i, _vp],
     "pbr_plain_resolve": [_vp, _vp, _vp, _vp],
+    "pbr_soft_config": [_vp, _f, _f, _i],
+    "pbr_node_set_grads": [_vp, _i, _vp, _vp, _vp, _vp],
+    "pbr_render_soft": [_vp, _vp, _vp, _vp],
+    "pbr_backward_soft": [_vp, _vp, _vp, _vp, _vp, _vp],
     "pbr_debug_transforms": [_vp, _i, _vp, _vp],
     "pbr_device_status": [_vp, ctypes.POINTER(ctypes.c_int32)],
 }

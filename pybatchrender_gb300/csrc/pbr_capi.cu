@@ -34,6 +34,7 @@ struct pbr_ctx {
   int bin_px = 16;
   int tri_cap_req = 0;
   int persistent = 0;
+  int kernel = 0;  // 0 auto, 1 scene-per-warp, 2 tile (CTA per scene region)
   // scratch
   int32_t* d_counter = nullptr;
   int32_t* d_status = nullptr;
@@ -41,6 +42,18 @@ struct pbr_ctx {
   uint32_t* d_cbuf = nullptr;
   // cudaFuncSetAttribute cache: [threads idx][plain][winner]
   int smem_set[3][2][2] = {};
+  int small_smem_set[2][2][2] = {};
+  int soft_smem_set[2][2] = {};
+  int soft_threads = 256;
+};
+
+// One launch configuration (what the autotuner searches over).
+struct LaunchCfg {
+  int kernel;  // 1 scene-per-warp, 2 tile; 0 = pick
+  int threads;
+  int bin_px;
+  int tri_cap;
+  int persistent;
 };
 
 static thread_local std::string g_create_err;
@@ -81,6 +94,8 @@ struct LaunchPlan {
   RasterArgs A;
   int smem = 0;
   int grid = 0;
+  int kind = 2;     // 1 scene-per-warp, 2 tile
+  int threads = 256;
 };
 
 static long long scene_source_tris(const pbr_ctx* ctx, int n0, int n1) {
@@ -92,8 +107,8 @@ static long long scene_source_tris(const pbr_ctx* ctx, int n0, int n1) {
   return s;
 }
 
-static int plan_launch(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int persistent, bool plain,
-                       bool winner, int n0, int n1, LaunchPlan* out) {
+static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int persistent, bool plain,
+                     bool winner, int n0, int n1, LaunchPlan* out) {
   const SceneParams& P = ctx->P;
   RasterArgs A;
   memset(&A, 0, sizeof(A));
@@ -174,7 +189,70 @@ static int plan_launch(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, i
     out->grid = A.num_items;
   }
   out->A = A;
+  out->kind = 2;
+  out->threads = threads;
   return PBR_OK;
+}
+
+// Scene-per-warp plan; returns PBR_ERR_CAPACITY when the scene is not small.
+static int plan_small(pbr_ctx* ctx, int threads, bool plain, bool winner, int n0, int n1, LaunchPlan* out) {
+  const SceneParams& P = ctx->P;
+  if (P.W % 16 != 0) return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp kernel needs width %% 16 == 0");
+  const long long need = 2 * scene_source_tris(ctx, n0, n1);
+  if (need > 128) return set_err(ctx, PBR_ERR_CAPACITY, "scene too large for the scene-per-warp kernel");
+  const int warps = threads >= 256 ? 8 : 4;
+  RasterArgs A;
+  memset(&A, 0, sizeof(A));
+  A.node_begin = n0;
+  A.node_end = n1;
+  A.tri_cap = std::max(32, (int)((need + 31) & ~31LL));
+  long long insts = 0, verts = 0;
+  for (int n = n0; n < n1; ++n) {
+    const NodeDesc& nd = P.nodes[n];
+    const MeshDesc& me = P.meshes[nd.mesh];
+    insts += nd.ips;
+    verts += (long long)nd.ips * me.nv;
+    if (me.smooth) A.smooth_any = 1;
+  }
+  if (insts > 32 || verts > 256)
+    return set_err(ctx, PBR_ERR_CAPACITY, "scene too large for the scene-per-warp kernel");
+  A.icap = std::max(1, (int)insts);
+  A.vcap = std::max(32, (int)((verts + 31) & ~31LL));
+  A.num_items = P.N;
+  A.status = ctx->d_status;
+  const int per_warp = pbr::small_smem_per_warp(A, P.W, P.H);
+  const int smem = per_warp * warps;
+  if (smem > ctx->max_smem) return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp layout exceeds shared memory");
+  int& cached = ctx->small_smem_set[warps == 8 ? 1 : 0][plain ? 1 : 0][winner ? 1 : 0];
+  if (smem > 48 * 1024 && smem > cached) {
+    cudaError_t e = pbr::small_set_smem_limit(warps, plain, winner, smem);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaFuncSetAttribute");
+    cached = smem;
+  }
+  out->A = A;
+  out->smem = smem;
+  out->grid = (P.N + warps - 1) / warps;
+  out->kind = 1;
+  out->threads = warps * 32;
+  return PBR_OK;
+}
+
+static int plan_any(pbr_ctx* ctx, const LaunchCfg& c, bool plain, bool winner, int n0, int n1, LaunchPlan* out) {
+  if (c.kernel == 1) return plan_small(ctx, c.threads, plain, winner, n0, n1, out);
+  if (c.kernel == 0) {
+    if (plan_small(ctx, c.threads, plain, winner, n0, n1, out) == PBR_OK) return PBR_OK;
+    ctx->err.clear();
+  }
+  return plan_tile(ctx, c.threads, c.bin_px, c.tri_cap, c.persistent, plain, winner, n0, n1, out);
+}
+
+static cudaError_t launch_plan(pbr_ctx* ctx, const LaunchPlan& lp, bool plain, bool winner, cudaStream_t s) {
+  if (lp.kind == 1) return pbr::small_launch(lp.threads / 32, plain, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
+  return pbr::hard_launch(lp.threads, plain, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
+}
+
+static LaunchCfg ctx_cfg(const pbr_ctx* ctx) {
+  return LaunchCfg{ctx->kernel, ctx->threads, ctx->bin_px, ctx->tri_cap_req, ctx->persistent};
 }
 
 static int check_ready(pbr_ctx* ctx, int n0, int n1) {
@@ -312,6 +390,7 @@ int pbr_node_set_buffers(pbr_ctx* ctx, int node_id, int mode, const float* d_pos
   if (!d_rot || !d_color) return set_err(ctx, PBR_ERR_INVALID, "rotation and colour buffers must be non-null");
   if (mode != pbr::kModeMat && (!d_pos || !d_scale))
     return set_err(ctx, PBR_ERR_INVALID, "position and scale buffers must be non-null");
+  if (((uintptr_t)d_color & 15u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_color must be 16-byte aligned");
   NodeDesc& nd = ctx->P.nodes[node_id];
   nd.mode = mode;
   nd.pos = d_pos;
@@ -358,8 +437,9 @@ int pbr_background_set(pbr_ctx* ctx, const float rgba[4]) {
   return PBR_OK;
 }
 
-int pbr_raster_config(pbr_ctx* ctx, int threads, int bin_px, int tri_cap, int persistent) {
+int pbr_raster_config(pbr_ctx* ctx, int kernel, int threads, int bin_px, int tri_cap, int persistent) {
   PBR_CHECK_CTX(ctx);
+  if (kernel < 0 || kernel > 2) return set_err(ctx, PBR_ERR_INVALID, "kernel must be 0 (auto), 1 or 2 (got %d)", kernel);
   if (threads != 128 && threads != 256 && threads != 512)
     return set_err(ctx, PBR_ERR_INVALID, "threads must be 128, 256 or 512 (got %d)", threads);
   if (bin_px != 8 && bin_px != 16 && bin_px != 32)
@@ -370,38 +450,42 @@ int pbr_raster_config(pbr_ctx* ctx, int threads, int bin_px, int tri_cap, int pe
   ctx->bin_px = bin_px;
   ctx->tri_cap_req = tri_cap;
   ctx->persistent = persistent ? 1 : 0;
+  ctx->kernel = kernel;
   return PBR_OK;
 }
 
-static int render_with(pbr_ctx* ctx, int threads, int bin_px, int tri_cap, int persistent, uint8_t* d_out,
-                       float* d_depth, int32_t* d_winner, cudaStream_t s) {
+static int render_with(pbr_ctx* ctx, const LaunchCfg& cfg, uint8_t* d_out, float* d_depth, int32_t* d_winner,
+                       cudaStream_t s) {
   LaunchPlan lp;
   const bool winner = d_winner != nullptr;
-  int rc = plan_launch(ctx, threads, bin_px, tri_cap, persistent, false, winner, 0, ctx->P.num_nodes, &lp);
+  int rc = plan_any(ctx, cfg, false, winner, 0, ctx->P.num_nodes, &lp);
   if (rc) return rc;
   lp.A.out = d_out;
   lp.A.depth = d_depth;
   lp.A.winner = d_winner;
-  if (persistent) {
+  if (lp.kind == 2 && lp.A.persistent) {
     cudaError_t e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMemsetAsync");
   }
-  cudaError_t e = pbr::hard_launch(threads, false, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
-  if (e != cudaSuccess) return cuda_err(ctx, e, "hard raster launch");
+  cudaError_t e = launch_plan(ctx, lp, false, winner, s);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "raster launch");
   return PBR_OK;
 }
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
 int pbr_render(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, int32_t* d_winner, void* stream) {
   PBR_CHECK_CTX(ctx);
   if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
+  if (!aligned16(d_out) || !aligned16(d_depth) || !aligned16(d_winner))
+    return set_err(ctx, PBR_ERR_INVALID, "output buffers must be 16-byte aligned");
   int rc = check_ready(ctx, 0, ctx->P.num_nodes);
   if (rc) return rc;
-  return render_with(ctx, ctx->threads, ctx->bin_px, ctx->tri_cap_req, ctx->persistent, d_out, d_depth, d_winner,
-                     (cudaStream_t)stream);
+  return render_with(ctx, ctx_cfg(ctx), d_out, d_depth, d_winner, (cudaStream_t)stream);
 }
 
-int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_threads, int* out_bin_px, int* out_tri_cap,
-                 int* out_persistent, float* out_ms) {
+int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_kernel, int* out_threads, int* out_bin_px,
+                 int* out_tri_cap, int* out_persistent, float* out_ms) {
   PBR_CHECK_CTX(ctx);
   if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
   int rc = check_ready(ctx, 0, ctx->P.num_nodes);
@@ -410,46 +494,50 @@ int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_threads, i
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int thr[3] = {128, 256, 512};
-  const int bins[3] = {8, 16, 32};
+  std::vector<LaunchCfg> cands;
+  {
+    LaunchPlan probe;
+    for (int t : {128, 256})
+      if (plan_small(ctx, t, false, false, 0, ctx->P.num_nodes, &probe) == PBR_OK) cands.push_back({1, t, 16, 0, 0});
+    ctx->err.clear();
+    const long long need = 2 * scene_source_tris(ctx, 0, ctx->P.num_nodes);
+    std::vector<int> caps = {0};
+    if (need > 256) { caps.push_back(256); caps.push_back(512); }
+    for (int t : {128, 256, 512})
+      for (int b : {8, 16, 32})
+        for (int p : {0, 1})
+          for (int cap : caps) cands.push_back({2, t, b, cap, p});
+  }
   float best = 1e30f;
-  int bt = ctx->threads, bb = ctx->bin_px, bp = ctx->persistent, bc = ctx->tri_cap_req;
-  const long long need = 2 * scene_source_tris(ctx, 0, ctx->P.num_nodes);
-  std::vector<int> caps = {0};
-  if (need > 256) { caps.push_back(256); caps.push_back(512); }
+  LaunchCfg bestc = ctx_cfg(ctx);
   int status = PBR_OK;
-  for (int ti = 0; ti < 3 && status == PBR_OK; ++ti)
-    for (int bi = 0; bi < 3 && status == PBR_OK; ++bi)
-      for (int pi = 0; pi < 2 && status == PBR_OK; ++pi)
-        for (int cap : caps) {
-          // warm-up + 3 timed launches
-          int r = render_with(ctx, thr[ti], bins[bi], cap, pi, d_out, nullptr, nullptr, s);
-          if (r == PBR_ERR_CAPACITY) { ctx->err.clear(); continue; }
-          if (r) { status = r; break; }
-          cudaEventRecord(e0, s);
-          for (int rep = 0; rep < 3; ++rep) render_with(ctx, thr[ti], bins[bi], cap, pi, d_out, nullptr, nullptr, s);
-          cudaEventRecord(e1, s);
-          cudaError_t ce = cudaEventSynchronize(e1);
-          if (ce != cudaSuccess) { status = cuda_err(ctx, ce, "autotune"); break; }
-          float ms = 0.f;
-          cudaEventElapsedTime(&ms, e0, e1);
-          ms /= 3.f;
-          if (ms < best) {
-            best = ms;
-            bt = thr[ti]; bb = bins[bi]; bp = pi; bc = cap;
-          }
-        }
+  for (const LaunchCfg& c : cands) {
+    int r = render_with(ctx, c, d_out, nullptr, nullptr, s);  // warm-up
+    if (r == PBR_ERR_CAPACITY) { ctx->err.clear(); continue; }
+    if (r) { status = r; break; }
+    cudaEventRecord(e0, s);
+    for (int rep = 0; rep < 3; ++rep) render_with(ctx, c, d_out, nullptr, nullptr, s);
+    cudaEventRecord(e1, s);
+    cudaError_t ce = cudaEventSynchronize(e1);
+    if (ce != cudaSuccess) { status = cuda_err(ctx, ce, "autotune"); break; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= 3.f;
+    if (ms < best) { best = ms; bestc = c; }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (status) return status;
-  ctx->threads = bt;
-  ctx->bin_px = bb;
-  ctx->persistent = bp;
-  ctx->tri_cap_req = bc;
-  if (out_threads) *out_threads = bt;
-  if (out_bin_px) *out_bin_px = bb;
-  if (out_tri_cap) *out_tri_cap = bc;
-  if (out_persistent) *out_persistent = bp;
+  ctx->kernel = bestc.kernel;
+  ctx->threads = bestc.threads;
+  ctx->bin_px = bestc.bin_px;
+  ctx->persistent = bestc.persistent;
+  ctx->tri_cap_req = bestc.tri_cap;
+  if (out_kernel) *out_kernel = bestc.kernel;
+  if (out_threads) *out_threads = bestc.threads;
+  if (out_bin_px) *out_bin_px = bestc.bin_px;
+  if (out_tri_cap) *out_tri_cap = bestc.tri_cap;
+  if (out_persistent) *out_persistent = bestc.persistent;
   if (out_ms) *out_ms = best;
   return PBR_OK;
 }
@@ -484,11 +572,13 @@ int pbr_plain_draw(pbr_ctx* ctx, int node_id, void* stream) {
   int rc = check_ready(ctx, node_id, node_id + 1);
   if (rc) return rc;
   LaunchPlan lp;
-  rc = plan_launch(ctx, 256, 16, 0, 0, true, false, node_id, node_id + 1, &lp);
+  LaunchCfg c = ctx_cfg(ctx);
+  c.persistent = 0;
+  rc = plan_any(ctx, c, true, false, node_id, node_id + 1, &lp);
   if (rc) return rc;
   lp.A.zbuf = ctx->d_zbuf;
   lp.A.cbuf = ctx->d_cbuf;
-  cudaError_t e = pbr::hard_launch(256, true, false, ctx->P, lp.A, lp.grid, lp.smem, (cudaStream_t)stream);
+  cudaError_t e = launch_plan(ctx, lp, true, false, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_err(ctx, e, "plain draw launch");
   return PBR_OK;
 }
@@ -499,6 +589,139 @@ int pbr_plain_resolve(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, void* stream
   if (!ctx->d_zbuf) return set_err(ctx, PBR_ERR_STATE, "pbr_plain_clear must run first");
   cudaError_t e = pbr::plain_resolve_launch(ctx->P, ctx->d_zbuf, ctx->d_cbuf, d_out, d_depth, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_err(ctx, e, "plain resolve launch");
+  return PBR_OK;
+}
+
+// ---------------------------------------------------------------------------
+// soft coverage
+
+static int plan_soft(pbr_ctx* ctx, int threads, bool backward, pbr::SoftArgs* out, int* smem_out, int* grid_out) {
+  const SceneParams& P = ctx->P;
+  pbr::SoftArgs A;
+  memset(&A, 0, sizeof(A));
+  const int HW = P.W * P.H;
+  const int bin_px = ctx->bin_px;
+  A.backward = backward ? 1 : 0;
+  A.region_px = threads * 8;
+  A.regions_per_scene = (HW + A.region_px - 1) / A.region_px;
+  A.num_items = P.N * A.regions_per_scene;
+  A.bin_px = bin_px;
+  A.bins_x = (P.W + bin_px - 1) / bin_px;
+  int mrb = 1;
+  for (int r = 0; r < A.regions_per_scene; ++r) {
+    const int p0 = r * A.region_px, p1 = std::min(p0 + A.region_px, HW);
+    mrb = std::max(mrb, ((p1 - 1) / P.W) / bin_px - (p0 / P.W) / bin_px + 1);
+  }
+  A.max_region_bins = mrb * A.bins_x;
+  int max_nv = 1;
+  long long max_inst_verts = 1, tris = 0, insts = 0;
+  for (int n = 0; n < P.num_nodes; ++n) {
+    const NodeDesc& nd = P.nodes[n];
+    const MeshDesc& me = P.meshes[nd.mesh];
+    max_nv = std::max(max_nv, me.nv);
+    max_inst_verts = std::max(max_inst_verts, (long long)nd.ips * me.nv);
+    tris += (long long)nd.ips * me.nt;
+    insts += nd.ips;
+  }
+  if (backward && insts > 1024)
+    return set_err(ctx, PBR_ERR_CAPACITY, "soft backward supports at most 1024 instances per scene (got %lld)", insts);
+  A.iacc_cap = backward ? (int)std::max<long long>(insts, 1) : 0;
+  A.vcap = (std::max(max_nv, (int)std::min<long long>(max_inst_verts, 512)) + 31) & ~31;
+  int icap = 1;
+  for (int n = 0; n < P.num_nodes; ++n) {
+    const NodeDesc& nd = P.nodes[n];
+    icap = std::max(icap, std::min(nd.ips, A.vcap / std::max(1, P.meshes[nd.mesh].nv)));
+  }
+  A.icap = std::min(icap, 128);
+  int cap = (int)std::min<long long>(std::max<long long>((tris + 31) & ~31LL, 32), 512);
+  A.status = ctx->d_status;
+  for (;;) {
+    A.tri_cap = cap;
+    const int bytes = pbr::soft_smem_bytes(A, threads);
+    if (bytes <= ctx->max_smem) {
+      *smem_out = bytes;
+      break;
+    }
+    if (cap > 32) {
+      cap = std::max(32, (cap / 2 + 31) & ~31);
+      continue;
+    }
+    if (A.vcap > max_nv) {
+      A.vcap = std::max((max_nv + 31) & ~31, A.vcap / 2);
+      A.icap = std::max(1, std::min(A.icap, A.vcap / max_nv));
+      continue;
+    }
+    return set_err(ctx, PBR_ERR_CAPACITY, "soft scene does not fit in shared memory (%d bytes needed)", bytes);
+  }
+  int& cached = ctx->soft_smem_set[threads == 256 ? 1 : 0][backward ? 1 : 0];
+  if (*smem_out > 48 * 1024 && *smem_out > cached) {
+    cudaError_t e = pbr::soft_set_smem_limit(threads, backward, *smem_out);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaFuncSetAttribute");
+    cached = *smem_out;
+  }
+  *grid_out = A.num_items;
+  *out = A;
+  return PBR_OK;
+}
+
+int pbr_soft_config(pbr_ctx* ctx, float sigma, float gamma, int threads) {
+  PBR_CHECK_CTX(ctx);
+  if (!(sigma > 0.f) || !(gamma > 0.f)) return set_err(ctx, PBR_ERR_INVALID, "sigma and gamma must be positive");
+  if (threads != 128 && threads != 256) return set_err(ctx, PBR_ERR_INVALID, "soft threads must be 128 or 256");
+  ctx->P.sigma = sigma;
+  ctx->P.gamma = gamma;
+  ctx->soft_threads = threads;
+  return PBR_OK;
+}
+
+int pbr_node_set_grads(pbr_ctx* ctx, int node_id, float* d_gpos, float* d_ghpr, float* d_gscale, float* d_gcol) {
+  PBR_CHECK_CTX(ctx);
+  if (node_id < 0 || node_id >= ctx->P.num_nodes) return set_err(ctx, PBR_ERR_INVALID, "unknown node id %d", node_id);
+  NodeDesc& nd = ctx->P.nodes[node_id];
+  nd.gpos = d_gpos;
+  nd.grot = d_ghpr;
+  nd.gscale = d_gscale;
+  nd.gcol = d_gcol;
+  return PBR_OK;
+}
+
+int pbr_render_soft(pbr_ctx* ctx, float* d_out, float* d_stats, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
+  if (((uintptr_t)d_stats & 7u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_stats must be 8-byte aligned");
+  int rc = check_ready(ctx, 0, ctx->P.num_nodes);
+  if (rc) return rc;
+  pbr::SoftArgs A;
+  int smem = 0, grid = 0;
+  rc = plan_soft(ctx, ctx->soft_threads, false, &A, &smem, &grid);
+  if (rc) return rc;
+  A.out = d_out;
+  A.stats = d_stats;
+  cudaError_t e = pbr::soft_launch(ctx->soft_threads, false, ctx->P, A, grid, smem, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "soft forward launch");
+  return PBR_OK;
+}
+
+int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, const float* d_grad_out,
+                      float* d_grad_light, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  if (!d_out || !d_stats || !d_grad_out) return set_err(ctx, PBR_ERR_INVALID, "d_out, d_stats and d_grad_out are required");
+  if (((uintptr_t)d_stats & 7u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_stats must be 8-byte aligned");
+  int rc = check_ready(ctx, 0, ctx->P.num_nodes);
+  if (rc) return rc;
+  for (int n = 0; n < ctx->P.num_nodes; ++n)
+    if (ctx->P.nodes[n].mode != pbr::kModeHpr)
+      return set_err(ctx, PBR_ERR_STATE, "soft backward needs every node in HPR mode (node %d is not)", n);
+  pbr::SoftArgs A;
+  int smem = 0, grid = 0;
+  rc = plan_soft(ctx, ctx->soft_threads, true, &A, &smem, &grid);
+  if (rc) return rc;
+  A.out = const_cast<float*>(d_out);
+  A.stats = const_cast<float*>(d_stats);
+  A.gout = d_grad_out;
+  A.glight = d_grad_light;
+  cudaError_t e = pbr::soft_launch(ctx->soft_threads, true, ctx->P, A, grid, smem, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "soft backward launch");
   return PBR_OK;
 }
 

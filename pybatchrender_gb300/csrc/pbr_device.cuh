@@ -1,0 +1,244 @@
+// pbr_device.cuh -- device helpers shared by the raster kernels: model
+// matrices (renderer/shader_context.py:47-84, renderer/node.py:116-126),
+// vertex/clip transforms (shaders/basic.vert:29-53), triangle setup with
+// watertight FP32 edge functions and the top-left rule, and the shading of
+// shaders/basic.frag:20-39.
+#pragma once
+
+#include "pbr_kernels.cuh"
+
+namespace pbr {
+
+__device__ __forceinline__ float clamp01f(float v) { return fminf(fmaxf(v, 0.f), 1.f); }
+
+__device__ __forceinline__ uint32_t unorm8(float v) {
+  return (uint32_t)floorf(clamp01f(v) * 255.f + 0.5f);
+}
+
+__device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a) {
+  return unorm8(r) | (unorm8(g) << 8) | (unorm8(b) << 16) | (unorm8(a) << 24);
+}
+
+// shaders/basic.frag:33-38 with base = 1 (no texture); n need not be unit length.
+__device__ __forceinline__ uint32_t shade_pack(const SceneParams& P, float nx, float ny, float nz, float4 col) {
+  float l2 = nx * nx + ny * ny + nz * nz;
+  float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
+  float ndl = (nx * P.ldir[0] + ny * P.ldir[1] + nz * P.ldir[2]) * inv;
+  ndl = fmaxf(ndl, 0.f);
+  const float s = P.strength;
+  float r = col.x * ((1.f - s) + (P.amb[0] + ndl * P.lcol[0]) * s);
+  float g = col.y * ((1.f - s) + (P.amb[1] + ndl * P.lcol[1]) * s);
+  float b = col.z * ((1.f - s) + (P.amb[2] + ndl * P.lcol[2]) * s);
+  return pack_rgba(r, g, b, col.w);
+}
+
+// shaders/basic.frag:33-38 without the UNORM8 clamp (soft mode: float output).
+__device__ __forceinline__ void shade_rgb(const SceneParams& P, float nx, float ny, float nz, float4 col, float out[3]) {
+  float l2 = nx * nx + ny * ny + nz * nz;
+  float inv = l2 > 0.f ? 1.f / sqrtf(l2) : 0.f;
+  float ndl = (nx * P.ldir[0] + ny * P.ldir[1] + nz * P.ldir[2]) * inv;
+  ndl = ndl > 0.f ? ndl : 0.f;
+  const float s = P.strength;
+  out[0] = col.x * ((1.f - s) + (P.amb[0] + ndl * P.lcol[0]) * s);
+  out[1] = col.y * ((1.f - s) + (P.amb[1] + ndl * P.lcol[1]) * s);
+  out[2] = col.z * ((1.f - s) + (P.amb[2] + ndl * P.lcol[2]) * s);
+}
+
+// Model matrix rows (3x4, row-major) of buffer row `id` of a node.
+__device__ __forceinline__ void build_model(const NodeDesc& nd, long long id, float m[12]) {
+  if (nd.mode == kModeMat) {
+    const float* s = nd.rot + id * 16;
+#pragma unroll
+    for (int i = 0; i < 12; ++i) m[i] = s[i];
+    return;
+  }
+  float R[9];
+  if (nd.mode == kModeHpr) {
+    const float* a = nd.rot + id * 3;
+    float sh, ch, sp, cp, sr, cr;
+    sincosf(a[0], &sh, &ch);
+    sincosf(a[1], &sp, &cp);
+    sincosf(a[2], &sr, &cr);
+    // Rz(H) @ Ry(P) @ Rx(R)
+    R[0] = ch * cp; R[1] = ch * sp * sr - sh * cr; R[2] = ch * sp * cr + sh * sr;
+    R[3] = sh * cp; R[4] = sh * sp * sr + ch * cr; R[5] = sh * sp * cr - ch * sr;
+    R[6] = -sp;     R[7] = cp * sr;                R[8] = cp * cr;
+  } else {
+    const float* a = nd.rot + id * 9;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = a[i];
+  }
+  const float s = nd.scale[id];
+  const float* p = nd.pos + id * 3;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    m[r * 4 + 0] = R[r * 3 + 0] * s;
+    m[r * 4 + 1] = R[r * 3 + 1] * s;
+    m[r * 4 + 2] = R[r * 3 + 2] * s;
+    m[r * 4 + 3] = p[r];
+  }
+}
+
+struct SV {
+  float x, y, z, iw;
+};
+
+__device__ __forceinline__ SV to_screen(float4 c, float W, float H) {
+  SV s;
+  s.iw = 1.f / c.w;
+  s.x = (c.x * s.iw + 1.f) * 0.5f * W;
+  s.y = (1.f - c.y * s.iw) * 0.5f * H;
+  s.z = c.z * s.iw * 0.5f + 0.5f;
+  return s;
+}
+
+// Per-item context for the triangle setup.
+struct SetupCtx {
+  float4* T0;
+  float4* T1;
+  float4* T2;
+  float4* T3;
+  float4* T4;
+  float4* S0;
+  float4* S1;
+  float4* S2;
+  float4* S3;
+  float W, H;
+  float ry0, ry1;  // region rows (inclusive)
+  int cull;
+};
+
+// Edge k of (v0,v1,v2) runs from v[(k+1)%3] to v[(k+2)%3].  Its function is
+// evaluated from the lexicographically smaller endpoint so that the two
+// triangles sharing an edge compute exactly negated values (watertight).
+__device__ __forceinline__ float4 make_edge(float xa, float ya, float xb, float yb, bool& tl) {
+  const bool a_first = (xa < xb) || (xa == xb && ya < yb);
+  const float xf = a_first ? xa : xb, yf = a_first ? ya : yb;
+  const float xs = a_first ? xb : xa, ys = a_first ? yb : ya;
+  float A = yf - ys, B = xs - xf;
+  if (!a_first) { A = -A; B = -B; }
+  tl = (A > 0.f) || (A == 0.f && B > 0.f);
+  return make_float4(A, B, xf, yf);
+}
+
+template <bool WRITE>
+__device__ __forceinline__ int setup_tri(const SceneParams& P, const SetupCtx& S, float4 c0, float4 n0, float4 c1,
+                                         float4 n1, float4 c2, float4 n2, int slot, float4 col, int draw_id,
+                                         bool smooth) {
+  SV v0 = to_screen(c0, S.W, S.H), v1 = to_screen(c1, S.W, S.H), v2 = to_screen(c2, S.W, S.H);
+  float area2 = (v1.x - v0.x) * (v2.y - v0.y) - (v2.x - v0.x) * (v1.y - v0.y);
+  if (S.cull) {
+    if (!(area2 < 0.f)) return 0;  // back-facing, degenerate or NaN
+  } else {
+    if (!(area2 < 0.f) && !(area2 > 0.f)) return 0;
+  }
+  if (area2 < 0.f) {
+    SV t = v1; v1 = v2; v2 = t;
+    float4 tn = n1; n1 = n2; n2 = tn;
+    area2 = -area2;
+  }
+  const float mnx = fminf(fminf(v0.x, v1.x), v2.x), mxx = fmaxf(fmaxf(v0.x, v1.x), v2.x);
+  const float mny = fminf(fminf(v0.y, v1.y), v2.y), mxy = fmaxf(fmaxf(v0.y, v1.y), v2.y);
+  // pixels whose centre can lie inside, widened by 1e-3 px (the edge test decides)
+  float fx0 = fmaxf(ceilf(mnx - 0.501f), 0.f), fx1 = fminf(floorf(mxx - 0.499f), S.W - 1.f);
+  float fy0 = fmaxf(ceilf(mny - 0.501f), S.ry0), fy1 = fminf(floorf(mxy - 0.499f), S.ry1);
+  if (!(fx0 <= fx1 && fy0 <= fy1)) return 0;
+  if (!WRITE) return 1;
+
+  bool tl0, tl1, tl2;
+  const float4 e0 = make_edge(v1.x, v1.y, v2.x, v2.y, tl0);
+  const float4 e1 = make_edge(v2.x, v2.y, v0.x, v0.y, tl1);
+  const float4 e2 = make_edge(v0.x, v0.y, v1.x, v1.y, tl2);
+  const float ia = 1.f / area2;
+  const float zA = (e0.x * v0.z + e1.x * v1.z + e2.x * v2.z) * ia;
+  const float zB = (e0.y * v0.z + e1.y * v1.z + e2.y * v2.z) * ia;
+  const float zC = v0.z - zA * v0.x - zB * v0.y;
+  const uint32_t xbox = (uint32_t)fx0 | ((uint32_t)fx1 << 16);
+  const uint32_t ybox = (uint32_t)fy0 | ((uint32_t)fy1 << 16);
+  const uint32_t flags = (tl0 ? 1u : 0u) | (tl1 ? 2u : 0u) | (tl2 ? 4u : 0u) | (smooth ? 8u : 0u);
+  const uint32_t color = smooth ? 0u : shade_pack(P, n0.x, n0.y, n0.z, col);
+  S.T0[slot] = e0;
+  S.T1[slot] = e1;
+  S.T2[slot] = e2;
+  S.T3[slot] = make_float4(zA, zB, zC, __uint_as_float(xbox));
+  S.T4[slot] = make_float4(__uint_as_float(ybox), __uint_as_float(flags), __uint_as_float(color),
+                           __int_as_float(draw_id));
+  if (smooth) {
+    S.S0[slot] = make_float4(n0.x, n0.y, n0.z, v0.iw);
+    S.S1[slot] = make_float4(n1.x, n1.y, n1.z, v1.iw);
+    S.S2[slot] = make_float4(n2.x, n2.y, n2.z, v2.iw);
+    S.S3[slot] = col;
+  }
+  return 1;
+}
+
+__device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
+  return make_float4(a.x + t * (b.x - a.x), a.y + t * (b.y - a.y), a.z + t * (b.z - a.z), a.w + t * (b.w - a.w));
+}
+
+// Near-plane clip (Sutherland-Hodgman against z + w >= 0: at most 4
+// vertices) and fan emission of a triangle that crosses the plane.  Crossing
+// points are interpolated from the endpoint with the smaller mesh index so
+// that neighbouring triangles produce identical vertices.  Its arrays live in
+// local memory, touched only on this rare path.
+template <bool WRITE>
+__device__ __forceinline__ int clip_tri(const SceneParams& P, const SetupCtx& S, float4 c0, float4 n0, float4 c1,
+                                     float4 n1, float4 c2, float4 n2, int i0, int i1, int i2, int slot, float4 col,
+                                     int draw_id, bool smooth) {
+  const float4 c[3] = {c0, c1, c2};
+  const float4 n[3] = {n0, n1, n2};
+  const int id[3] = {i0, i1, i2};
+  const float d[3] = {c0.z + c0.w, c1.z + c1.w, c2.z + c2.w};
+  float4 pc[4], pn[4];
+  int np = 0;
+#pragma unroll
+  for (int e = 0; e < 3; ++e) {
+    const int a = e, b = (e + 1) % 3;
+    const bool ina = d[a] >= 0.f, inb = d[b] >= 0.f;
+    if (ina) { pc[np] = c[a]; pn[np] = n[a]; ++np; }
+    if (ina != inb) {
+      const int f = id[a] < id[b] ? a : b, s = id[a] < id[b] ? b : a;
+      const float t = d[f] / (d[f] - d[s]);
+      pc[np] = lerp4(c[f], c[s], t);
+      pn[np] = lerp4(n[f], n[s], t);
+      ++np;
+    }
+  }
+  int cnt = 0;
+  for (int f = 1; f + 1 < np; ++f)
+    cnt += setup_tri<WRITE>(P, S, pc[0], pn[0], pc[f], pn[f], pc[f + 1], pn[f + 1], slot + cnt, col, draw_id, smooth);
+  return cnt;
+}
+
+// One source triangle: returns the number of screen triangles emitted at
+// slot, slot+1 (0, 1, or 2 after near-plane clipping).
+template <bool WRITE>
+__device__ __forceinline__ int process_tri(const SceneParams& P, const SetupCtx& S, const float4* vcache, int vbase,
+                                           int i0, int i1, int i2, int slot, float4 col, int draw_id, bool smooth) {
+  const float4 c0 = vcache[2 * (vbase + i0)], n0 = vcache[2 * (vbase + i0) + 1];
+  const float4 c1 = vcache[2 * (vbase + i1)], n1 = vcache[2 * (vbase + i1) + 1];
+  const float4 c2 = vcache[2 * (vbase + i2)], n2 = vcache[2 * (vbase + i2) + 1];
+  const float d0 = c0.z + c0.w, d1 = c1.z + c1.w, d2 = c2.z + c2.w;
+  if (d0 >= 0.f && d1 >= 0.f && d2 >= 0.f)
+    return setup_tri<WRITE>(P, S, c0, n0, c1, n1, c2, n2, slot, col, draw_id, smooth);
+  if (d0 < 0.f && d1 < 0.f && d2 < 0.f) return 0;
+  return clip_tri<WRITE>(P, S, c0, n0, c1, n1, c2, n2, i0, i1, i2, slot, col, draw_id, smooth);
+}
+
+// Per-pixel smooth shading of chunk triangle t at pixel centre (px, py).
+__device__ __forceinline__ uint32_t shade_smooth(const SceneParams& P, const SetupCtx& S, int t, float px, float py) {
+  const float4 e0 = S.T0[t], e1 = S.T1[t], e2 = S.T2[t];
+  const float E0 = fmaf(e0.x, px - e0.z, e0.y * (py - e0.w));
+  const float E1 = fmaf(e1.x, px - e1.z, e1.y * (py - e1.w));
+  const float E2 = fmaf(e2.x, px - e2.z, e2.y * (py - e2.w));
+  const float4 a0 = S.S0[t], a1 = S.S1[t], a2 = S.S2[t];
+  // perspective-correct interpolation; the common 1/area2 and 1/sum factors
+  // cancel in the normalisation of shade_pack
+  const float q0 = E0 * a0.w, q1 = E1 * a1.w, q2 = E2 * a2.w;
+  const float nx = q0 * a0.x + q1 * a1.x + q2 * a2.x;
+  const float ny = q0 * a0.y + q1 * a1.y + q2 * a2.y;
+  const float nz = q0 * a0.z + q1 * a1.z + q2 * a2.z;
+  return shade_pack(P, nx, ny, nz, S.S3[t]);
+}
+
+}  // namespace pbr

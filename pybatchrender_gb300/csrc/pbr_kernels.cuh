@@ -37,8 +37,9 @@ struct NodeDesc {
   const float* rot;       // [B,3] | [B,9] | [B,16]
   const float* scale;     // [B]
   const float* color;     // [B,4]
-  float* gpos;            // soft-mode gradients (may be null)
-  float* grot;
+  float* gpos;            // soft-mode gradients, accumulated (may be null)
+  float* grot;            // d/d(heading, pitch, roll)
+  float* gscale;
   float* gcol;
   int32_t mesh, ips, shared, mode;
   int32_t rank_base, pad0, pad1, pad2;
@@ -76,6 +77,24 @@ struct RasterArgs {
   int32_t persistent;
   int32_t smooth_any;
   int32_t multi_chunk;
+};
+
+// Soft-coverage launch arguments (pbr_soft.cu).
+struct SoftArgs {
+  float* out;          // forward: [N,3,H,W] output; backward: the forward's output (read)
+  float* stats;        // [N,H,W,2] (log-sum-exp, coverage code): written by forward, read by backward
+  const float* gout;   // backward: dL/dout [N,3,H,W]
+  float* glight;       // backward: dL/d(normalised light direction) [3], accumulated
+  int32_t* status;
+  int32_t tri_cap, vcap, icap, iacc_cap;
+  int32_t region_px, regions_per_scene, num_items;
+  int32_t bin_px, bins_x, max_region_bins;
+  int32_t backward;
+};
+
+struct SoftLayout {
+  int rec[15];
+  int masks, vcache, vidx, icache, state, tacc, iacc, misc, total;
 };
 
 // Shared-memory carve-up, identical on host (to size the launch) and device.

@@ -14,6 +14,17 @@ cudaError_t hard_set_smem_limit(int threads, bool plain, bool winner, int bytes)
 cudaError_t hard_occupancy(int threads, bool plain, bool winner, int smem_bytes, int* blocks_per_sm);
 cudaError_t hard_launch(int threads, bool plain, bool winner, const SceneParams& P, const RasterArgs& A,
                         int grid, int smem_bytes, cudaStream_t stream);
+// Scene-per-warp raster (pbr_small.cu); warps in {4, 8}.
+int small_smem_per_warp(const RasterArgs& A, int W, int H);
+cudaError_t small_set_smem_limit(int warps, bool plain, bool winner, int bytes);
+cudaError_t small_occupancy(int warps, bool plain, bool winner, int smem_bytes, int* blocks_per_sm);
+cudaError_t small_launch(int warps, bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int grid,
+                         int smem_bytes, cudaStream_t stream);
+// Soft coverage (pbr_soft.cu); threads in {128, 256}.
+int soft_smem_bytes(const SoftArgs& a, int threads);
+cudaError_t soft_set_smem_limit(int threads, bool backward, int bytes);
+cudaError_t soft_launch(int threads, bool backward, const SceneParams& P, const SoftArgs& A, int grid, int smem_bytes,
+                        cudaStream_t stream);
 cudaError_t plain_clear_launch(const SceneParams& P, float* zbuf, uint32_t* cbuf, cudaStream_t stream);
 cudaError_t plain_resolve_launch(const SceneParams& P, const float* zbuf, const uint32_t* cbuf, uint8_t* out,
                                  float* depth, cudaStream_t stream);

@@ -107,14 +107,16 @@ class PBRNode(PBRShaderContext):
         (``node.py:128-134``)."""
         if not self.has_geometry:
             return
-        self.pos.copy_(self._as(pos_si3, 3)[:self.buf_instances])
+        with torch.no_grad():
+            self.pos.copy_(self._as(pos_si3, 3)[:self.buf_instances])
 
     def set_hprs(self, hpr_si3, lazy: bool = False) -> None:
         """Instance heading/pitch/roll in radians, ``R = Rz(H) Ry(P) Rx(R)``
         (``node.py:136-143``)."""
         if not self.has_geometry:
             return
-        self.hpr.copy_(self._as(hpr_si3, 3)[:self.buf_instances])
+        with torch.no_grad():
+            self.hpr.copy_(self._as(hpr_si3, 3)[:self.buf_instances])
         if self.mode != MODE_HPR:
             self.mode = MODE_HPR
             self._rebind()
@@ -125,15 +127,18 @@ class PBRNode(PBRShaderContext):
         if not self.has_geometry:
             return
         if isinstance(scale_si1, (float, int)):
-            self.scale.fill_(float(scale_si1))
+            with torch.no_grad():
+                self.scale.fill_(float(scale_si1))
         else:
-            self.scale.copy_(self._as(scale_si1, None)[:self.buf_instances])
+            with torch.no_grad():
+                self.scale.copy_(self._as(scale_si1, None)[:self.buf_instances])
 
     def set_colors(self, col_si4) -> None:
         """Per-instance RGBA (``node.py:156-161``)."""
         if not self.has_geometry:
             return
-        self.color.copy_(self._as(col_si4, 4)[:self.buf_instances])
+        with torch.no_grad():
+            self.color.copy_(self._as(col_si4, 4)[:self.buf_instances])
 
     def set_transforms(self, mats_b44) -> None:
         """Full per-instance matrices (B,4,4).  As in ``node.py:163-178`` the
@@ -150,9 +155,10 @@ class PBRNode(PBRShaderContext):
         B = self.buf_instances
         if self.rot3 is None:
             self.rot3 = torch.zeros((B, 3, 3), dtype=torch.float32, device=self.device)
-        self.rot3.copy_((rot3 / s.reshape(-1, 1, 1))[:B])
-        self.scale.copy_(s[:B])
-        self.pos.copy_(mats[:, 0:3, 3][:B])
+        with torch.no_grad():
+            self.rot3.copy_((rot3 / s.reshape(-1, 1, 1))[:B])
+            self.scale.copy_(s[:B])
+            self.pos.copy_(mats[:, 0:3, 3][:B])
         if self.mode != MODE_ROT:
             self.mode = MODE_ROT
             self._rebind()

@@ -36,6 +36,9 @@ from .light import PBRLight
 from .node import MODE_MAT, PBRNode, mesh_key
 
 
+KERNELS = {"auto": 0, "warp": 1, "tile": 2}
+
+
 class PBRRenderer:
     """Batch renderer for ``num_scenes`` independent scenes."""
 
@@ -146,6 +149,8 @@ class PBRRenderer:
         if not getattr(self.cfg, "interactive", False):
             self._step(*args, **kwargs)
         if return_pixels:
+            if self.cfg.raster_mode == "soft":
+                return self.render_soft()
             return self.render()
         return None
 
@@ -193,6 +198,58 @@ class PBRRenderer:
         if return_winner:
             res.append(winner)
         return res[0] if len(res) == 1 else tuple(res)
+
+    # ------------------------------------------------------------ soft mode
+    def render_soft(self, light_dir: torch.Tensor | None = None) -> torch.Tensor:
+        """Soft-coverage render, float32 ``[N,3,H,W]``.  Differentiable when
+        autograd is enabled and a node tensor (``pos``, ``hpr``, ``scale``,
+        ``color``) or ``light_dir`` requires grad."""
+        from .soft import soft_params, soft_render
+        self._require_ready()
+        params = soft_params(self)
+        if torch.is_grad_enabled() and (any(p.requires_grad for p in params)
+                                        or (light_dir is not None and light_dir.requires_grad)):
+            return soft_render(self, light_dir)
+        out, _ = self._soft_forward(light_dir, want_stats=False)
+        return out
+
+    def _soft_forward(self, light_dir: torch.Tensor | None, want_stats: bool = True):
+        if light_dir is not None:
+            self._set_light_direction(light_dir)
+        N, C, H, W = self._out_shape()
+        out = torch.empty((N, 3, H, W), dtype=torch.float32, device=self.device)
+        stats = torch.empty((N, H, W, 2), dtype=torch.float32, device=self.device) if want_stats else None
+        _capi.call(self._lib, self._ctx, "pbr_render_soft", _capi.ptr(out), _capi.ptr(stats), self._stream())
+        return out, stats
+
+    def _soft_backward(self, out: torch.Tensor, stats: torch.Tensor, gout: torch.Tensor):
+        """Run the adjoint kernel; returns ([(gpos, ghpr, gscale, gcol) per
+        node], dL/d normalised light direction)."""
+        grads = []
+        for node, nid in self._node_ids.items():
+            B = node.buf_instances
+            g = (torch.zeros((B, 3), dtype=torch.float32, device=self.device),
+                 torch.zeros((B, 3), dtype=torch.float32, device=self.device),
+                 torch.zeros((B,), dtype=torch.float32, device=self.device),
+                 torch.zeros((B, 4), dtype=torch.float32, device=self.device))
+            _capi.call(self._lib, self._ctx, "pbr_node_set_grads", nid, *[_capi.ptr(t) for t in g])
+            grads.append(g)
+        g_light = torch.zeros(3, dtype=torch.float32, device=self.device)
+        try:
+            _capi.call(self._lib, self._ctx, "pbr_backward_soft", _capi.ptr(out), _capi.ptr(stats), _capi.ptr(gout),
+                       _capi.ptr(g_light), self._stream())
+        finally:
+            for nid in self._node_ids.values():
+                _capi.call(self._lib, self._ctx, "pbr_node_set_grads", nid, None, None, None, None)
+        return grads, g_light
+
+    def _set_light_direction(self, light_dir: torch.Tensor) -> None:
+        d = [float(v) for v in torch.as_tensor(light_dir).detach().cpu().reshape(3).tolist()]
+        if self._pbr_light is None:
+            self.add_light()
+        light = self._pbr_light
+        if tuple(d) != tuple(light.dir_dir):
+            light.set_directional(d, light.dir_col)
 
     def _render_plain(self, want_depth: bool):
         """The reference's per-step flow on the GPU: per node, host matrices
@@ -251,12 +308,16 @@ class PBRRenderer:
         self._require_ready()
         N, C, H, W = self._out_shape()
         scratch = torch.empty((N, C, H, W), dtype=torch.uint8, device=self.device)
-        vals = [ctypes.c_int() for _ in range(4)]
+        vals = [ctypes.c_int() for _ in range(5)]
         ms = ctypes.c_float()
         _capi.call(self._lib, self._ctx, "pbr_autotune", _capi.ptr(scratch), self._stream(),
                    *[ctypes.byref(v) for v in vals], ctypes.byref(ms))
-        self.autotune_result = {"threads": vals[0].value, "bin_px": vals[1].value, "tri_cap": vals[2].value,
-                                "persistent": vals[3].value, "ms": ms.value}
+        names = {v: k for k, v in KERNELS.items()}
+        self.autotune_result = {"kernel": names[vals[0].value], "threads": vals[1].value, "bin_px": vals[2].value,
+                                "tri_cap": vals[3].value, "persistent": vals[4].value, "ms": ms.value}
+        c = self.cfg
+        c.raster_kernel, c.raster_threads, c.bin_size = names[vals[0].value], vals[1].value, vals[2].value
+        c.tri_cap, c.persistent = vals[3].value, bool(vals[4].value)
         self._graph = None
         return self.autotune_result
 
@@ -360,8 +421,10 @@ class PBRRenderer:
             self._camera_changed(self._pbr_cam)
             self._light_changed(self._pbr_light)
             _capi.call(lib, ctx, "pbr_background_set", (ctypes.c_float * 4)(*self._background_color))
-            _capi.call(lib, ctx, "pbr_raster_config", int(self.cfg.raster_threads), int(self.cfg.bin_size),
-                       int(self.cfg.tri_cap), int(bool(self.cfg.persistent)))
+            _capi.call(lib, ctx, "pbr_raster_config", KERNELS[self.cfg.raster_kernel], int(self.cfg.raster_threads),
+                       int(self.cfg.bin_size), int(self.cfg.tri_cap), int(bool(self.cfg.persistent)))
+            _capi.call(lib, ctx, "pbr_soft_config", float(self.cfg.soft_sigma), float(self.cfg.soft_gamma),
+                       128 if int(self.cfg.raster_threads) == 128 else 256)
 
     def _bind_node_buffers(self, node: PBRNode) -> None:
         nid = self._node_ids[node]

@@ -43,7 +43,7 @@ def test_cartpole_bench_256_parity(cuda, oracle):
     r = workloads.cartpole_bench(num_scenes=256, res=64, seed=1)
     r._step(workloads.cartpole_states(256, seed=2, device=cuda))
     cmp, gpu, ref = check_parity(r, oracle)
-    assert (ref["winner"] >= 0).mean() > 0.01  # the scene is not empty
+    assert (ref["winner"] >= 0).mean() > 0.002  # the scene is not empty (small objects by design)
     assert cmp["ambiguous"] < 0.01 * cmp["pixels"]
 
 
@@ -171,7 +171,9 @@ def test_near_plane_clipping(cuda, oracle):
     r.add_light()
     # two-sided: the big cube is seen from inside, so its back faces are culled like GL does
     r.setup_environment()
-    cmp, gpu, ref = check_parity(r, oracle)
+    # window depth of near-plane-clipped triangles (vertices far off-screen) is
+    # only good to ~1e-3 in FP32; coverage and depth order must still match
+    cmp, gpu, ref = check_parity(r, oracle, depth_tol=1e-3)
 
 
 def test_empty_and_degenerate_inputs(cuda, oracle):
@@ -207,3 +209,57 @@ def test_env_step_renders(cuda):
     td = env.step(td)
     assert td["next", "pixels"].shape == (32, 3, 64, 64)
     assert td["next", "pixels"].float().mean() > 0
+
+
+@pytest.mark.parametrize("kernel", ["warp", "tile"])
+def test_cartpole_both_kernels_parity(cuda, oracle, kernel):
+    r = workloads.cartpole_bench(num_scenes=96, res=64, seed=21, raster_kernel=kernel)
+    r._step(workloads.cartpole_states(96, seed=22, device=cuda))
+    check_parity(r, oracle)
+
+
+def test_warp_and_tile_kernels_bitwise_equal(cuda):
+    st = workloads.cartpole_states(200, seed=23, device=cuda)
+    # pixels and winners identical; window depth equal up to FMA contraction
+    # differences between the two kernel bodies
+    outs = []
+    for kernel in ("warp", "tile"):
+        r = workloads.cartpole_bench(num_scenes=200, res=64, seed=24, raster_kernel=kernel)
+        r._step(st)
+        outs.append(r.render(return_depth=True, return_winner=True))
+    (pa, da, wa), (pb, db, wb) = outs
+    assert torch.equal(pa, pb) and torch.equal(wa, wb)
+    assert torch.allclose(da, db, rtol=0, atol=1e-6)
+    outs = []
+    for kernel in ("warp", "tile"):
+        r = CartPoleRenderer(CartPoleConfig(num_scenes=40, raster_kernel=kernel))
+        r._step(st[:40])
+        outs.append(r.render(return_depth=True))
+    assert torch.equal(outs[0][0], outs[1][0])
+    assert torch.allclose(outs[0][1], outs[1][1], rtol=0, atol=1e-6)
+
+
+@pytest.mark.parametrize("res", [(48, 20), (16, 16), (96, 40)])
+def test_warp_kernel_ragged_bins(cuda, oracle, res):
+    """Widths that are multiples of 16 but not of 32, heights not multiple of 16."""
+    r = pbr.PBRRenderer(num_scenes=7, tile_resolution=res, raster_kernel="warp")
+    node = r.add_node("models/box", 3, model_pivot_relative_point=(0.5, 0.5, 0.5))
+    g = torch.Generator().manual_seed(25)
+    node.set_positions(torch.rand((21, 3), generator=g) * 3 - 1.5)
+    node.set_hprs(torch.rand((21, 3), generator=g) * 6.3)
+    node.set_colors(torch.rand((21, 4), generator=g))
+    r.add_camera(fov_y_deg=50)
+    r._pbr_cam.set_positions_and_lookat([0.0, -7.0, 1.0], [0.0, 0.0, 0.0])
+    r.add_light()
+    r.set_background_color(0.2, 0.3, 0.4)
+    r.setup_environment()
+    check_parity(r, oracle)
+
+
+def test_plain_tile_kernel_matches(cuda):
+    st = workloads.cartpole_states(32, seed=26)
+    a = workloads.cartpole_bench(num_scenes=32, seed=27, raster_kernel="tile")
+    b = workloads.cartpole_bench(num_scenes=32, seed=27, raster_method="plain", raster_kernel="tile")
+    a._step(st.to(cuda))
+    b._step(st)
+    assert torch.equal(a.render(), b.render())

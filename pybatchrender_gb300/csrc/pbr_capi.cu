@@ -688,7 +688,7 @@ int pbr_node_set_grads(pbr_ctx* ctx, int node_id, float* d_gpos, float* d_ghpr, 
 int pbr_render_soft(pbr_ctx* ctx, float* d_out, float* d_stats, void* stream) {
   PBR_CHECK_CTX(ctx);
   if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
-  if (((uintptr_t)d_stats & 7u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_stats must be 8-byte aligned");
+  if (((uintptr_t)d_stats & 15u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_stats must be 16-byte aligned");
   int rc = check_ready(ctx, 0, ctx->P.num_nodes);
   if (rc) return rc;
   pbr::SoftArgs A;
@@ -706,7 +706,7 @@ int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, co
                       float* d_grad_light, void* stream) {
   PBR_CHECK_CTX(ctx);
   if (!d_out || !d_stats || !d_grad_out) return set_err(ctx, PBR_ERR_INVALID, "d_out, d_stats and d_grad_out are required");
-  if (((uintptr_t)d_stats & 7u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_stats must be 8-byte aligned");
+  if (((uintptr_t)d_stats & 15u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_stats must be 16-byte aligned");
   int rc = check_ready(ctx, 0, ctx->P.num_nodes);
   if (rc) return rc;
   for (int n = 0; n < ctx->P.num_nodes; ++n)

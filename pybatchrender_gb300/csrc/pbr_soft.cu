@@ -13,8 +13,10 @@
 //   w_j  = D_j exp((zs_j - max zs) / gamma),   A = 1 - prod_j (1 - D_j)
 //   out  = A sum_j w_j C_j / sum_j w_j + (1 - A) bg
 //
-// The forward also stores per-pixel statistics (log-sum-exp L = m + gamma ln S
-// and a code for prod(1 - D)) so the adjoint needs a single sweep: it
+// The forward also stores per-pixel statistics (the running max m of zs, the
+// softmax denominator S relative to it -- kept apart because m + gamma ln S in
+// float32 would lose m's precision 1/gamma-fold -- and a code for
+// prod(1 - D)) so the adjoint needs a single sweep: it
 // recomputes every tile's fragment list from the triangle setup (nothing
 // per-fragment is stored), accumulates per-triangle gradients with warp
 // reductions, chains them through the viewport / projection / model matrix
@@ -40,7 +42,7 @@ __host__ __device__ inline SoftLayout soft_layout(const SoftArgs& a, int threads
   L.vcache = off; off += align16(a.vcap * 32);
   L.vidx = off; off += align16(a.vcap * 4);
   L.icache = off; off += align16(a.icap * 64);
-  L.state = off; off += align16(threads * kSPx * (a.backward ? 10 : 7) * 4);
+  L.state = off; off += align16(threads * kSPx * (a.backward ? 11 : 7) * 4);
   if (a.backward) {
     L.tacc = off; off += align16(a.tri_cap * 24 * 4);
     L.iacc = off; off += align16(a.iacc_cap * kIacc * 4);
@@ -181,7 +183,7 @@ __device__ __forceinline__ bool soft_frag(const SceneParams& P, const SoftCtx& S
   f.Q = f.E[0] * iw.x + f.E[1] * iw.y + f.E[2] * iw.z;
   if (!(f.Q > 0.f)) return false;
 #pragma unroll
-  for (int k = 0; k < 3; ++k) f.sg[k] = 1.f / (1.f + __expf(-f.e[k] * inv_sigma));
+  for (int k = 0; k < 3; ++k) f.sg[k] = 1.f / (1.f + expf(-f.e[k] * inv_sigma));
   f.Ds = f.sg[0] * f.sg[1] * f.sg[2];
   float T = 1.f;
   f.dTdd = 0.f;
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
     const bool active = q0 < p1;
 
     // ---- per-pixel state ---------------------------------------------------
-    // forward: m, S, acc0..2, Pnz, nz      backward: L, Pnz, nz, A, Cfg0..2, dLdCfg0..2
+    // forward: m, S, acc0..2, Pnz, nz      backward: m, Pnz, nz, A, Cfg0..2, dLdCfg0..2, 1/S
 #pragma unroll
     for (int j = 0; j < kSPx; ++j) {
       const int q = q0 + j;
@@ -318,11 +320,12 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
         ST(0, j) = -1e30f; ST(1, j) = 0.f; ST(2, j) = 0.f; ST(3, j) = 0.f; ST(4, j) = 0.f;
         ST(5, j) = 1.f; ST(6, j) = 0.f;
       } else {
-        float Lv = -1e30f, code = 1.f, Av = 0.f, cf[3] = {0.f, 0.f, 0.f}, g[3] = {0.f, 0.f, 0.f};
+        float Lv = -1e30f, Sv = 1.f, code = 1.f, Av = 0.f, cf[3] = {0.f, 0.f, 0.f}, g[3] = {0.f, 0.f, 0.f};
         if (active && q < p1) {
-          const float2 stv = *reinterpret_cast<const float2*>(A.stats + 2 * ((long long)k * HW + q));
+          const float4 stv = *reinterpret_cast<const float4*>(A.stats + 4 * ((long long)k * HW + q));
           Lv = stv.x;
-          code = stv.y;
+          Sv = stv.y;
+          code = stv.z;
           float Pnz, nz;
           if (code >= 0.f) { Pnz = code; nz = 0.f; } else if (code >= -2.f) { Pnz = -1.f - code; nz = 1.f; } else { Pnz = 0.f; nz = 2.f; }
           Av = nz > 0.f ? 1.f : 1.f - Pnz;
@@ -340,6 +343,7 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
         }
         ST(0, j) = Lv;
         ST(3, j) = Av;
+        ST(10, j) = Sv > 0.f ? 1.f / Sv : 0.f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           ST(4 + c, j) = cf[c];
@@ -428,14 +432,14 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
               if (1.f - f.D == 0.f) ST(6, j) += 1.f;
               else ST(5, j) *= (1.f - f.D);
               if (f.zs > m0) {
-                const float sc = __expf((m0 - f.zs) * inv_gamma);
+                const float sc = expf((m0 - f.zs) * inv_gamma);
                 ST(1, j) = S0 * sc + f.D;
                 ST(2, j) = ST(2, j) * sc + f.D * f.C[0];
                 ST(3, j) = ST(3, j) * sc + f.D * f.C[1];
                 ST(4, j) = ST(4, j) * sc + f.D * f.C[2];
                 ST(0, j) = f.zs;
               } else {
-                const float wv = f.D * __expf((f.zs - m0) * inv_gamma);
+                const float wv = f.D * expf((f.zs - m0) * inv_gamma);
                 ST(1, j) = S0 + wv;
                 ST(2, j) += wv * f.C[0];
                 ST(3, j) += wv * f.C[1];
@@ -478,7 +482,7 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
                 // dL/dA = g . (Cfg - bg); g = dLdCfg / A
                 float dLdA = 0.f;
                 if (Av > 0.f) dLdA = (dc0 * (cf0 - P.bg[0]) + dc1 * (cf1 - P.bg[1]) + dc2 * (cf2 - P.bg[2])) / Av;
-                const float ewn = __expf((f.zs - Lp) * inv_gamma);
+                const float ewn = expf((f.zs - Lp) * inv_gamma) * ST(10, j);
                 const float wn = f.D * ewn;
                 const float dCx = wn * dc0, dCy = wn * dc1, dCz = wn * dc2;
                 const float dws = dc0 * (f.C[0] - cf0) + dc1 * (f.C[1] - cf1) + dc2 * (f.C[2] - cf2);
@@ -744,8 +748,7 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
           if (A.stats) {
             // coverage code: prod over non-zero (1 - D), folded with the count of zero factors
             const float code = nz == 0.f ? Pv : (nz == 1.f ? -1.f - Pv : -3.f);
-            const float Lv = S0 > 0.f ? m0 + P.gamma * __logf(S0) : -1e30f;
-            *reinterpret_cast<float2*>(A.stats + 2 * ((long long)k * HW + q)) = make_float2(Lv, code);
+            *reinterpret_cast<float4*>(A.stats + 4 * ((long long)k * HW + q)) = make_float4(m0, S0, code, 0.f);
           }
         }
       }

@@ -1,0 +1,135 @@
+"""Host-side API behaviour (CPU only): registry, node/camera/light setters,
+error conventions, and that rendering without a CUDA device fails loudly."""
+import os
+import warnings
+
+import numpy as np
+import pytest
+import torch
+
+import pybatchrender_gb300 as pbr
+from pybatchrender_gb300 import envs, workloads
+from pybatchrender_gb300.env import PBREnv, TensorDictLite
+from pybatchrender_gb300.envs.cartpole import CartPoleConfig, CartPoleEnv, CartPoleRenderer
+from pybatchrender_gb300.renderer import meshes
+
+
+def test_public_names():
+    for name in ("PBRConfig", "PBRRenderer", "PBRNode", "PBRCam", "PBRLight", "PBRShaderContext", "PBREnv", "envs"):
+        assert getattr(pbr, name) is not None
+    assert pbr.GPUFrameGrabber is None and pbr.CPUFrameGrabber is None
+
+
+def test_registry():
+    assert "CartPole-v0" in envs.list_envs() and envs.is_registered("CartPole-v0")
+    env_cls, r_cls, c_cls = envs.get_env_classes("CartPole-v0")
+    assert (env_cls, r_cls, c_cls) == (CartPoleEnv, CartPoleRenderer, CartPoleConfig)
+    with pytest.raises(ValueError):
+        envs.get_env_classes("Nope-v0")
+    with pytest.raises(ValueError):
+        envs.make("Nope-v0")
+    envs.register("Tmp-v0", CartPoleEnv, CartPoleRenderer, CartPoleConfig)
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        envs.register("Tmp-v0", CartPoleEnv, CartPoleRenderer, CartPoleConfig)
+        assert any("already registered" in str(x.message) for x in w)
+    envs.unregister("Tmp-v0")
+    assert not envs.is_registered("Tmp-v0")
+
+
+def test_rendering_without_cuda_raises():
+    r = workloads.cartpole_bench(num_scenes=4, device="cpu")
+    with pytest.raises(pbr.RendererUnavailable):
+        r.step(workloads.cartpole_states(4, seed=0))
+    with pytest.raises(pbr.RendererUnavailable):
+        r.render_soft()
+
+
+def test_node_setter_semantics():
+    r = pbr.PBRRenderer(num_scenes=3, device="cpu")
+    n = r.add_node("models/box", 2)
+    assert n.buf_instances == 6 and n.total_instances == 6
+    n.set_positions(torch.tensor([1.0, 2.0, 3.0]))  # a single row broadcasts
+    assert torch.equal(n.pos, torch.tensor([[1.0, 2.0, 3.0]]).repeat(6, 1))
+    n.set_positions(np.arange(24, dtype=np.float32).reshape(8, 3))  # extra rows are ignored
+    assert torch.equal(n.pos, torch.arange(18, dtype=torch.float32).reshape(6, 3))
+    n.set_scales(2.5)
+    assert torch.all(n.scale == 2.5)
+    n.set_hprs(torch.zeros((6, 3)))
+    n.set_colors([0.1, 0.2, 0.3, 1.0])
+    assert torch.allclose(n.color[3], torch.tensor([0.1, 0.2, 0.3, 1.0]))
+    M = n.get_transforms()
+    assert torch.allclose(M[:, :3, :3], torch.eye(3).expand(6, 3, 3) * 2.5)
+    s = pbr.PBRRenderer(num_scenes=3, device="cpu").add_node("models/box", 2, shared_across_scenes=True)
+    assert s.buf_instances == 2
+    with pytest.raises(NotImplementedError):
+        r.add_node("models/box", 1, backend="loop")
+    with pytest.raises(NotImplementedError):
+        r.add_node("models/box", 1, texture="tex.png")
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        r.add_node("models/box", 1, positions=torch.zeros(3))
+        assert any("ignored" in str(x.message) for x in w)
+    empty = r.add_node(None, 1)
+    empty.set_positions(torch.zeros(3))  # no geometry: a no-op
+    assert not empty.has_geometry
+    with pytest.raises(NotImplementedError):
+        n.reparent_to(empty)
+
+
+def test_camera_errors_and_light():
+    r = pbr.PBRRenderer(num_scenes=4, device="cpu")
+    cam = r.add_camera()
+    with pytest.raises(ValueError):
+        cam.set_eye(torch.zeros((3, 3)))
+    with pytest.raises(ValueError):
+        cam.set_eye(torch.zeros((4, 2)))
+    with pytest.raises(NotImplementedError):
+        cam.set_positions(torch.zeros(3), keep_lookat=True)
+    cam.set_projection(fov_y_deg=30.0)
+    assert cam.P_k44[1, 1] == pytest.approx(1.0 / np.tan(np.radians(15.0)), rel=1e-6)
+    light = r.add_light(strength=0.5)
+    light.set_ambient((0.3, 0.3, 0.3))
+    assert light.ambient == (0.3, 0.3, 0.3) and light.strength == 0.5
+
+
+def test_meshes_and_baking():
+    box = meshes.resolve_model("models/box")
+    assert box.num_vertices == 24 and box.num_triangles == 12 and not box.smooth
+    assert meshes.cylinder(64).num_triangles == 256 and meshes.icosphere(3).num_triangles == 1280
+    b = meshes.bake(box, (0.1, 0.1, 2.0), None, (0.5, 0.5, 0.05))
+    lo, hi = b.tight_bounds()
+    assert np.allclose(lo, [-0.05, -0.05, -0.1]) and np.allclose(hi, [0.05, 0.05, 1.9])
+    a = meshes.bake(box, 0.3, None, None, "absolute")
+    assert np.allclose(a.tight_bounds()[1] - a.tight_bounds()[0], 0.3)
+    with pytest.raises(ValueError):
+        meshes.bake(box, (1.0, 2.0), None, None)
+    with pytest.raises(FileNotFoundError):
+        meshes.resolve_model("models/smiley")
+
+
+def test_env_without_renderer_pixels():
+    cfg = CartPoleConfig(num_scenes=8, device="cpu", render=False)
+    r = CartPoleRenderer(cfg)
+    env = CartPoleEnv(r, cfg)
+    td = env.reset()
+    assert td["observation"].shape == (8, 4) and "pixels" not in td
+    td["action"] = env.action_spec.rand()
+    td = env.step(td)
+    nxt = td["next"]
+    assert nxt["observation"].shape == (8, 4) and nxt["reward"].shape == (8, 1)
+    assert nxt["done"].dtype == torch.bool
+
+
+def test_tensordict_lite_nested_keys():
+    td = TensorDictLite({"a": torch.zeros(2)}, batch_size=[2])
+    td[("next", "b")] = torch.ones(2)
+    assert torch.equal(td["next", "b"], torch.ones(2)) and td.get("missing") is None
+
+
+def test_atlas_roundtrip():
+    r = pbr.PBRRenderer(num_scenes=5, tile_resolution=(8, 6), device="cpu")
+    pix = torch.randint(0, 255, (5, 3, 6, 8), dtype=torch.uint8)
+    atlas = r.to_atlas(pix)
+    assert atlas.shape == (2 * 6, 3 * 8, 3)
+    assert torch.equal(r._rearrange_img(atlas), pix)

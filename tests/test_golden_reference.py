@@ -1,0 +1,107 @@
+"""The package and the oracle against fixtures recorded from the reference's
+own scene code (tests/golden/make_golden.py runs it under stand-in Panda3D
+modules and records what it would upload to OpenGL).  CPU only."""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import pybatchrender_gb300 as pbr
+from oracle import oracle
+from pybatchrender_gb300.envs.cartpole import CartPoleConfig, CartPoleRenderer
+from tests.golden import scenes
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def sorted_rows(a):
+    a = np.round(np.asarray(a, np.float64), 5)
+    return a[np.lexsort(a.T[::-1])]
+
+
+def test_config_resolution_matches_reference():
+    cases = json.load(open(os.path.join(GOLDEN, "ref_config_cases.json")))
+    assert len(cases) == len(scenes.CONFIG_CASES)
+    for case in cases:
+        kw = {k: tuple(v) if isinstance(v, list) else v for k, v in case["kwargs"].items()}
+        if "error" in case:
+            with pytest.raises(Exception) as ei:
+                pbr.PBRConfig(device="cpu", **kw)
+            assert type(ei.value).__name__ == case["error"], case
+            continue
+        c = pbr.PBRConfig(device="cpu", **kw)
+        assert list(c.tiles) == case["tiles"], case
+        assert list(c.tile_resolution) == case["tile_resolution"], case
+        assert list(c.window_resolution) == case["window_resolution"], case
+        assert c.num_scenes == case["num_scenes"] and c.batch_inner_dim == case["batch_inner_dim"], case
+
+
+@pytest.mark.parametrize("N", [5, 64, 4098])
+def test_cartpole_buffers_match_reference(N):
+    ref = load(f"ref_cartpole_N{N}.npz")
+    r = CartPoleRenderer(CartPoleConfig(num_scenes=N, device="cpu"))
+    r._step(torch.tensor(ref["state"]))
+    sel = ref["sel"] if "sel" in ref else np.arange(N)
+    assert tuple(r.cfg.tiles) == tuple(ref["tiles_cfg"]) and tuple(r.cfg.window_resolution) == tuple(ref["window"])
+    for name in ("rail", "cart", "pole"):
+        node = getattr(r, name)
+        M = node.get_transforms().numpy()
+        rows = sel if not node.shared_across else np.arange(node.buf_instances)
+        want = ref[f"{name}_M"] if node.shared_across else ref[f"{name}_M"]
+        got = M[rows] if not node.shared_across else M
+        assert np.allclose(got, want, rtol=1e-6, atol=1e-6), name
+        colr = node.color.numpy()
+        assert np.array_equal(colr[rows] if not node.shared_across else colr, ref[f"{name}_color"]), name
+        assert np.allclose(sorted_rows(node.mesh.positions), sorted_rows(ref[f"{name}_verts"]), atol=1e-5), name
+        assert int(ref[f"{name}_in_shareAcrossScenes"]) == int(node.shared_across)
+        assert int(ref[f"{name}_in_K"]) == N
+        assert tuple(ref[f"{name}_in_screenSize"]) == tuple(float(v) for v in r.cfg.window_resolution)
+        light = r._pbr_light
+        assert np.allclose(ref[f"{name}_in_dirLightDir"], light.dir_dir)
+        assert np.allclose(ref[f"{name}_in_ambientCol"], light.ambient)
+        assert float(ref[f"{name}_in_lightingStrength"]) == light.strength
+    cam = r._pbr_cam
+    assert np.allclose(cam.P_k44.numpy(), ref["P"], rtol=1e-7, atol=0)
+    assert np.allclose(cam.VP_k44.numpy()[sel], ref["VP"], rtol=1e-6, atol=1e-6)
+    assert np.array_equal(cam.tiles_k4.numpy()[sel], ref["tiles"])
+
+
+def test_api_scene_matches_reference():
+    ref = load("ref_api_scene.npz")
+    r, snaps = scenes.api_scene(pbr, device="cpu")
+    for name, node in zip("abc", r.nodes_abc):
+        assert np.allclose(node.get_transforms().numpy(), ref[f"{name}_M"], rtol=1e-5, atol=1e-6), name
+        assert np.array_equal(node.color.numpy(), ref[f"{name}_color"]), name
+        assert np.allclose(sorted_rows(node.mesh.positions), sorted_rows(ref[f"{name}_verts"]), atol=1e-5), name
+    for label, vp in snaps:
+        assert np.allclose(vp.numpy(), ref[f"snap_{label}"], rtol=1e-5, atol=1e-5), label
+    light = r._pbr_light
+    assert np.allclose(ref["light"], light.ambient + light.dir_dir + light.dir_col + (light.strength,))
+    assert np.array_equal(r._pbr_cam.tiles_k4.numpy(), ref["tiles"])
+
+
+@pytest.mark.parametrize("N", [5, 64])
+def test_oracle_matrices_match_reference(N):
+    """The oracle's model-matrix builder (oracle/raster_ref.c) against the
+    reference's CPU torch matrices for the same poses."""
+    ref = load(f"ref_cartpole_N{N}.npz")
+    r = CartPoleRenderer(CartPoleConfig(num_scenes=N, device="cpu"))
+    r._step(torch.tensor(ref["state"]))
+    for name in ("rail", "cart", "pole"):
+        node = getattr(r, name)
+        got = oracle.instance_matrices(dict(node.export(), mesh=0))
+        assert np.allclose(got, ref[f"{name}_M"], rtol=1e-6, atol=1e-6), name
+
+
+def test_api_scene_oracle_matrices_match_reference():
+    ref = load("ref_api_scene.npz")
+    r, _ = scenes.api_scene(pbr, device="cpu")
+    for name, node in zip("abc", r.nodes_abc):
+        got = oracle.instance_matrices(dict(node.export(), mesh=0))
+        assert np.allclose(got, ref[f"{name}_M"], rtol=1e-5, atol=1e-6), name

@@ -714,13 +714,14 @@ int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, co
       return set_err(ctx, PBR_ERR_STATE, "soft backward needs every node in HPR mode (node %d is not)", n);
   pbr::SoftArgs A;
   int smem = 0, grid = 0;
-  rc = plan_soft(ctx, ctx->soft_threads, true, &A, &smem, &grid);
+  // the adjoint keeps 15 values per pixel in shared memory: 128-thread CTAs
+  rc = plan_soft(ctx, 128, true, &A, &smem, &grid);
   if (rc) return rc;
   A.out = const_cast<float*>(d_out);
   A.stats = const_cast<float*>(d_stats);
   A.gout = d_grad_out;
   A.glight = d_grad_light;
-  cudaError_t e = pbr::soft_launch(ctx->soft_threads, true, ctx->P, A, grid, smem, (cudaStream_t)stream);
+  cudaError_t e = pbr::soft_launch(128, true, ctx->P, A, grid, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_err(ctx, e, "soft backward launch");
   return PBR_OK;
 }

@@ -82,7 +82,7 @@ struct RasterArgs {
 // Soft-coverage launch arguments (pbr_soft.cu).
 struct SoftArgs {
   float* out;          // forward: [N,3,H,W] output; backward: the forward's output (read)
-  float* stats;        // [N,H,W,4] (max zs, softmax denominator, coverage code, -): forward writes, backward reads
+  float* stats;        // [N,H,W,8] (max zs, softmax denominator, coverage code, -, Cfg - C_r (3), -)
   const float* gout;   // backward: dL/dout [N,3,H,W]
   float* glight;       // backward: dL/d(normalised light direction) [3], accumulated
   int32_t* status;

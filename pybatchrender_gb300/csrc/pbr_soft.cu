@@ -13,10 +13,13 @@
 //   w_j  = D_j exp((zs_j - max zs) / gamma),   A = 1 - prod_j (1 - D_j)
 //   out  = A sum_j w_j C_j / sum_j w_j + (1 - A) bg
 //
-// The forward also stores per-pixel statistics (the running max m of zs, the
-// softmax denominator S relative to it -- kept apart because m + gamma ln S in
-// float32 would lose m's precision 1/gamma-fold -- and a code for
-// prod(1 - D)) so the adjoint needs a single sweep: it
+// Colours are accumulated relative to the first fragment's colour C_r, so that
+// C_j - Cfg, which the adjoint multiplies by 1/gamma, is exactly 0 where all
+// fragments share a colour (the faces of a flat-shaded mesh).  The forward
+// stores per-pixel statistics (the running max m of zs, the softmax
+// denominator S relative to it -- kept apart because m + gamma ln S in float32
+// would lose m's precision 1/gamma-fold --, a code for prod(1 - D), and
+// Cfg - C_r) so the adjoint needs a single sweep: it
 // recomputes every tile's fragment list from the triangle setup (nothing
 // per-fragment is stored), accumulates per-triangle gradients with warp
 // reductions, chains them through the viewport / projection / model matrix
@@ -42,7 +45,7 @@ __host__ __device__ inline SoftLayout soft_layout(const SoftArgs& a, int threads
   L.vcache = off; off += align16(a.vcap * 32);
   L.vidx = off; off += align16(a.vcap * 4);
   L.icache = off; off += align16(a.icap * 64);
-  L.state = off; off += align16(threads * kSPx * (a.backward ? 11 : 7) * 4);
+  L.state = off; off += align16(threads * kSPx * (a.backward ? 15 : 11) * 4);
   if (a.backward) {
     L.tacc = off; off += align16(a.tri_cap * 24 * 4);
     L.iacc = off; off += align16(a.iacc_cap * kIacc * 4);
@@ -312,20 +315,26 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
     const bool active = q0 < p1;
 
     // ---- per-pixel state ---------------------------------------------------
-    // forward: m, S, acc0..2, Pnz, nz      backward: m, Pnz, nz, A, Cfg0..2, dLdCfg0..2, 1/S
+    // forward:  m, S, acc0..2 (relative to C_r), Pnz, nz, C_r0..2, has_ref
+    // backward: m, Pnz, nz, dL/dA, Cfg-C_r 0..2, dLdCfg0..2, 1/S, C_r0..2, has_ref
 #pragma unroll
     for (int j = 0; j < kSPx; ++j) {
       const int q = q0 + j;
       if (!BACKWARD) {
         ST(0, j) = -1e30f; ST(1, j) = 0.f; ST(2, j) = 0.f; ST(3, j) = 0.f; ST(4, j) = 0.f;
-        ST(5, j) = 1.f; ST(6, j) = 0.f;
+        ST(5, j) = 1.f; ST(6, j) = 0.f; ST(7, j) = 0.f; ST(8, j) = 0.f; ST(9, j) = 0.f; ST(10, j) = 0.f;
       } else {
         float Lv = -1e30f, Sv = 1.f, code = 1.f, Av = 0.f, cf[3] = {0.f, 0.f, 0.f}, g[3] = {0.f, 0.f, 0.f};
+        float dl[3] = {0.f, 0.f, 0.f};
         if (active && q < p1) {
-          const float4 stv = *reinterpret_cast<const float4*>(A.stats + 4 * ((long long)k * HW + q));
+          const float4 stv = *reinterpret_cast<const float4*>(A.stats + 8 * ((long long)k * HW + q));
+          const float4 stw = *reinterpret_cast<const float4*>(A.stats + 8 * ((long long)k * HW + q) + 4);
           Lv = stv.x;
           Sv = stv.y;
           code = stv.z;
+          dl[0] = stw.x;
+          dl[1] = stw.y;
+          dl[2] = stw.z;
           float Pnz, nz;
           if (code >= 0.f) { Pnz = code; nz = 0.f; } else if (code >= -2.f) { Pnz = -1.f - code; nz = 1.f; } else { Pnz = 0.f; nz = 2.f; }
           Av = nz > 0.f ? 1.f : 1.f - Pnz;
@@ -342,11 +351,14 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
           ST(2, j) = 0.f;
         }
         ST(0, j) = Lv;
-        ST(3, j) = Av;
+        // dL/dA = g . (Cfg - bg); Cfg from the output is accurate enough here
+        // (this term is not amplified by 1/gamma)
+        ST(3, j) = g[0] * (cf[0] - P.bg[0]) + g[1] * (cf[1] - P.bg[1]) + g[2] * (cf[2] - P.bg[2]);
         ST(10, j) = Sv > 0.f ? 1.f / Sv : 0.f;
+        ST(14, j) = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          ST(4 + c, j) = cf[c];
+          ST(4 + c, j) = dl[c];
           ST(7 + c, j) = Av * g[c];
         }
       }
@@ -431,19 +443,26 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
               float m0 = ST(0, j), S0 = ST(1, j);
               if (1.f - f.D == 0.f) ST(6, j) += 1.f;
               else ST(5, j) *= (1.f - f.D);
+              if (ST(10, j) == 0.f) {  // first fragment: the colour reference
+                ST(7, j) = f.C[0];
+                ST(8, j) = f.C[1];
+                ST(9, j) = f.C[2];
+                ST(10, j) = 1.f;
+              }
+              const float d0 = f.C[0] - ST(7, j), d1 = f.C[1] - ST(8, j), d2 = f.C[2] - ST(9, j);
               if (f.zs > m0) {
                 const float sc = expf((m0 - f.zs) * inv_gamma);
                 ST(1, j) = S0 * sc + f.D;
-                ST(2, j) = ST(2, j) * sc + f.D * f.C[0];
-                ST(3, j) = ST(3, j) * sc + f.D * f.C[1];
-                ST(4, j) = ST(4, j) * sc + f.D * f.C[2];
+                ST(2, j) = ST(2, j) * sc + f.D * d0;
+                ST(3, j) = ST(3, j) * sc + f.D * d1;
+                ST(4, j) = ST(4, j) * sc + f.D * d2;
                 ST(0, j) = f.zs;
               } else {
                 const float wv = f.D * expf((f.zs - m0) * inv_gamma);
                 ST(1, j) = S0 + wv;
-                ST(2, j) += wv * f.C[0];
-                ST(3, j) += wv * f.C[1];
-                ST(4, j) += wv * f.C[2];
+                ST(2, j) += wv * d0;
+                ST(3, j) += wv * d1;
+                ST(4, j) += wv * d2;
               }
             }
           } else {
@@ -476,16 +495,20 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
                 Frag f;
                 if (!soft_frag(P, S, t, px, py, inv_sigma, inv_zr, f)) continue;
                 const float Lp = ST(0, j), Pnz = ST(1, j), nz = ST(2, j);
-                const float cf0 = ST(4, j), cf1 = ST(5, j), cf2 = ST(6, j);
+                if (ST(14, j) == 0.f) {  // first fragment: the colour reference of the forward
+                  ST(11, j) = f.C[0];
+                  ST(12, j) = f.C[1];
+                  ST(13, j) = f.C[2];
+                  ST(14, j) = 1.f;
+                }
                 const float dc0 = ST(7, j), dc1 = ST(8, j), dc2 = ST(9, j);
-                const float Av = ST(3, j);
-                // dL/dA = g . (Cfg - bg); g = dLdCfg / A
-                float dLdA = 0.f;
-                if (Av > 0.f) dLdA = (dc0 * (cf0 - P.bg[0]) + dc1 * (cf1 - P.bg[1]) + dc2 * (cf2 - P.bg[2])) / Av;
+                const float dLdA = ST(3, j);
                 const float ewn = expf((f.zs - Lp) * inv_gamma) * ST(10, j);
                 const float wn = f.D * ewn;
                 const float dCx = wn * dc0, dCy = wn * dc1, dCz = wn * dc2;
-                const float dws = dc0 * (f.C[0] - cf0) + dc1 * (f.C[1] - cf1) + dc2 * (f.C[2] - cf2);
+                // C_j - Cfg = (C_j - C_r) - (Cfg - C_r)
+                const float dws = dc0 * ((f.C[0] - ST(11, j)) - ST(4, j)) + dc1 * ((f.C[1] - ST(12, j)) - ST(5, j)) +
+                                  dc2 * ((f.C[2] - ST(13, j)) - ST(6, j));
                 const float omd = 1.f - f.D;
                 float dAdD = 0.f;
                 if (nz == 0.f) dAdD = Pnz / omd;
@@ -740,15 +763,19 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
           if (q >= p1) continue;
           const float m0 = ST(0, j), S0 = ST(1, j), Pv = ST(5, j), nz = ST(6, j);
           const float Av = 1.f - (nz > 0.f ? 0.f : Pv);
+          float dl[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const float fg = S0 > 0.f ? ST(2 + c, j) / S0 : 0.f;
+            dl[c] = S0 > 0.f ? ST(2 + c, j) / S0 : 0.f;  // Cfg - C_r
+            const float fg = ST(7 + c, j) + dl[c];
             A.out[((long long)k * 3 + c) * HW + q] = Av * fg + (1.f - Av) * P.bg[c];
           }
           if (A.stats) {
             // coverage code: prod over non-zero (1 - D), folded with the count of zero factors
             const float code = nz == 0.f ? Pv : (nz == 1.f ? -1.f - Pv : -3.f);
-            *reinterpret_cast<float4*>(A.stats + 4 * ((long long)k * HW + q)) = make_float4(m0, S0, code, 0.f);
+            float4* so = reinterpret_cast<float4*>(A.stats + 8 * ((long long)k * HW + q));
+            so[0] = make_float4(m0, S0, code, 0.f);
+            so[1] = make_float4(dl[0], dl[1], dl[2], 0.f);
           }
         }
       }

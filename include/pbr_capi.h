@@ -171,6 +171,20 @@ int pbr_render_soft(pbr_ctx* ctx, float* d_out, float* d_stats, void* stream);
 int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, const float* d_grad_out,
                       float* d_grad_light, void* stream);
 
+/* The plain per-node render (clear, one draw per node, resolve) with its
+ * depth/colour scratch in a static 16 MiB device array instead of a
+ * cudaMalloc'd buffer: for callers that may not allocate device memory when
+ * they render -- inside a CUDA stream capture, or under a host framework whose
+ * allocator owns the device memory.  This call allocates nothing; the
+ * context is created beforehand.  Limit: num_scenes * width * height at most
+ * about 2M pixels (8 bytes each); larger requests fail with PBR_ERR_CAPACITY.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress): make it once before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU (other streams, other
+ * contexts) race; calls on one stream are ordered.  No counterpart in the
+ * reference. */
+int pbr_plain_render_noalloc(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, void* stream);
+
 /* Model matrices the kernels build for one node: d_out [B,16] row-major.
  * For tests; replaces reading back matbuf (renderer/node.py:110-126). */
 int pbr_debug_transforms(pbr_ctx* ctx, int node_id, float* d_out, void* stream);

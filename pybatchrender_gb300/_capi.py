@@ -45,6 +45,7 @@ SIGNATURES: dict[str, list] = {
     "pbr_plain_clear": [_vp, _vp],
     "pbr_plain_draw": [_vp, _i, _vp],
     "pbr_plain_resolve": [_vp, _vp, _vp, _vp],
+    "pbr_plain_render_noalloc": [_vp, _vp, _vp, _vp],
     "pbr_soft_config": [_vp, _f, _f, _i],
     "pbr_node_set_grads": [_vp, _i, _vp, _vp, _vp, _vp],
     "pbr_render_soft": [_vp, _vp, _vp, _vp],

@@ -753,3 +753,79 @@ int pbr_device_status(pbr_ctx* ctx, int32_t* out_flags) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Plain per-node render without any allocation.
+//
+// pbr_plain_clear allocates the plain path's depth/colour buffer with
+// cudaMalloc on first use.  Callers that may not allocate device memory at
+// render time -- a render issued while a CUDA stream is being captured (an
+// allocation there invalidates the capture), or a host framework whose
+// allocator has already reserved the device memory and forbids raw
+// cudaMalloc -- use pbr_plain_render_noalloc instead.  Its scratch is a
+// file-scope device array that exists from the moment the library is loaded
+// (every GPU that loads libpbr.so holds it until the process exits), so the
+// call itself allocates nothing.
+#include <mutex>
+
+#define PBR_NOALLOC_SCRATCH_BYTES (16u << 20)  // 16 MiB: N*H*W*8 bytes (plus alignment) must fit
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PBR_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_base[256];  // device address of g_noalloc_scratch, per device ordinal
+
+extern "C" int pbr_plain_render_noalloc(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
+  int rc = check_ready(ctx, 0, ctx->P.num_nodes);
+  if (rc) return rc;
+  const size_t px = (size_t)ctx->P.N * ctx->P.W * ctx->P.H;
+  const size_t cofs = (px * sizeof(float) + 255) & ~(size_t)255;  // colour buffer after the depth buffer
+  const size_t need = cofs + px * sizeof(uint32_t);
+  if (need > PBR_NOALLOC_SCRATCH_BYTES)
+    return set_err(ctx, PBR_ERR_CAPACITY,
+                   "pbr_plain_render_noalloc needs %zu bytes of scratch for %zu pixels; its static buffer holds %u "
+                   "bytes (at most about %u pixels: num_scenes * width * height)",
+                   need, px, (unsigned)PBR_NOALLOC_SCRATCH_BYTES, (unsigned)(PBR_NOALLOC_SCRATCH_BYTES / 8));
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "cudaGetDevice");
+  if (dev != ctx->device)
+    return set_err(ctx, PBR_ERR_STATE, "the context's device (%d) must be current (current: %d)", ctx->device, dev);
+  if (dev < 0 || dev >= 256) return set_err(ctx, PBR_ERR_INVALID, "device ordinal %d out of range", dev);
+  void* base = nullptr;
+  {
+    // first call on this device: look up the array's device address (a host
+    // reference to g_noalloc_scratch is only a stand-in, not a device address)
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_base[dev]) {
+      e = cudaGetSymbolAddress(&g_noalloc_base[dev], g_noalloc_scratch);
+      if (e != cudaSuccess) {
+        g_noalloc_base[dev] = nullptr;
+        return cuda_err(ctx, e, "cudaGetSymbolAddress");
+      }
+    }
+    base = g_noalloc_base[dev];
+  }
+  float* zbuf = reinterpret_cast<float*>(base);
+  uint32_t* cbuf = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(base) + cofs);
+  cudaStream_t s = (cudaStream_t)stream;
+  // every pixel of the used range is written by the clear: no stale state survives
+  e = pbr::plain_clear_launch(ctx->P, zbuf, cbuf, s);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "plain clear launch");
+  LaunchCfg c = ctx_cfg(ctx);
+  c.persistent = 0;
+  for (int n = 0; n < ctx->P.num_nodes; ++n) {
+    LaunchPlan lp;
+    rc = plan_any(ctx, c, true, false, n, n + 1, &lp);
+    if (rc) return rc;
+    lp.A.zbuf = zbuf;
+    lp.A.cbuf = cbuf;
+    e = launch_plan(ctx, lp, true, false, s);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "plain draw launch");
+  }
+  e = pbr::plain_resolve_launch(ctx->P, zbuf, cbuf, d_out, d_depth, s);
+  if (e != cudaSuccess) return cuda_err(ctx, e, "plain resolve launch");
+  return PBR_OK;
+}

@@ -195,17 +195,17 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
 }
 
 // Scene-per-warp plan; returns PBR_ERR_CAPACITY when the scene is not small.
-static int plan_small(pbr_ctx* ctx, int threads, bool plain, bool winner, int n0, int n1, LaunchPlan* out) {
+static int plan_small(pbr_ctx* ctx, bool plain, bool winner, int n0, int n1, LaunchPlan* out) {
   const SceneParams& P = ctx->P;
   if (P.W % 16 != 0) return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp kernel needs width %% 16 == 0");
-  const long long need = 2 * scene_source_tris(ctx, n0, n1);
+  const long long need = 2 * scene_source_tris(ctx, n0, n1);  // a near-plane clip can split a triangle in two
   if (need > 128) return set_err(ctx, PBR_ERR_CAPACITY, "scene too large for the scene-per-warp kernel");
-  const int warps = threads >= 256 ? 8 : 4;
+  const int warps = pbr::small_warps();
   RasterArgs A;
   memset(&A, 0, sizeof(A));
   A.node_begin = n0;
   A.node_end = n1;
-  A.tri_cap = std::max(32, (int)((need + 31) & ~31LL));
+  A.tri_cap = std::max(16, (int)((need + 15) & ~15LL));
   long long insts = 0, verts = 0;
   for (int n = n0; n < n1; ++n) {
     const NodeDesc& nd = P.nodes[n];
@@ -217,15 +217,16 @@ static int plan_small(pbr_ctx* ctx, int threads, bool plain, bool winner, int n0
   if (insts > 32 || verts > 256)
     return set_err(ctx, PBR_ERR_CAPACITY, "scene too large for the scene-per-warp kernel");
   A.icap = std::max(1, (int)insts);
-  A.vcap = std::max(32, (int)((verts + 31) & ~31LL));
+  A.vcap = std::max(1, (int)verts);
   A.num_items = P.N;
   A.status = ctx->d_status;
   const int per_warp = pbr::small_smem_per_warp(A, P.W, P.H);
+  if (per_warp < 0) return set_err(ctx, PBR_ERR_CAPACITY, "image too large for the scene-per-warp kernel");
   const int smem = per_warp * warps;
   if (smem > ctx->max_smem) return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp layout exceeds shared memory");
-  int& cached = ctx->small_smem_set[warps == 8 ? 1 : 0][plain ? 1 : 0][winner ? 1 : 0];
+  int& cached = ctx->small_smem_set[plain ? 1 : 0][winner ? 1 : 0][A.smooth_any ? 1 : 0];
   if (smem > 48 * 1024 && smem > cached) {
-    cudaError_t e = pbr::small_set_smem_limit(warps, plain, winner, smem);
+    cudaError_t e = pbr::small_set_smem_limit(plain, winner, A.smooth_any != 0, smem);
     if (e != cudaSuccess) return cuda_err(ctx, e, "cudaFuncSetAttribute");
     cached = smem;
   }
@@ -238,16 +239,16 @@ static int plan_small(pbr_ctx* ctx, int threads, bool plain, bool winner, int n0
 }
 
 static int plan_any(pbr_ctx* ctx, const LaunchCfg& c, bool plain, bool winner, int n0, int n1, LaunchPlan* out) {
-  if (c.kernel == 1) return plan_small(ctx, c.threads, plain, winner, n0, n1, out);
+  if (c.kernel == 1) return plan_small(ctx, plain, winner, n0, n1, out);
   if (c.kernel == 0) {
-    if (plan_small(ctx, c.threads, plain, winner, n0, n1, out) == PBR_OK) return PBR_OK;
+    if (plan_small(ctx, plain, winner, n0, n1, out) == PBR_OK) return PBR_OK;
     ctx->err.clear();
   }
   return plan_tile(ctx, c.threads, c.bin_px, c.tri_cap, c.persistent, plain, winner, n0, n1, out);
 }
 
 static cudaError_t launch_plan(pbr_ctx* ctx, const LaunchPlan& lp, bool plain, bool winner, cudaStream_t s) {
-  if (lp.kind == 1) return pbr::small_launch(lp.threads / 32, plain, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
+  if (lp.kind == 1) return pbr::small_launch(plain, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
   return pbr::hard_launch(lp.threads, plain, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
 }
 
@@ -497,8 +498,8 @@ int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_kernel, in
   std::vector<LaunchCfg> cands;
   {
     LaunchPlan probe;
-    for (int t : {128, 256})
-      if (plan_small(ctx, t, false, false, 0, ctx->P.num_nodes, &probe) == PBR_OK) cands.push_back({1, t, 16, 0, 0});
+    if (plan_small(ctx, false, false, 0, ctx->P.num_nodes, &probe) == PBR_OK)
+      cands.push_back({1, pbr::small_warps() * 32, 16, 0, 0});
     ctx->err.clear();
     const long long need = 2 * scene_source_tris(ctx, 0, ctx->P.num_nodes);
     std::vector<int> caps = {0};

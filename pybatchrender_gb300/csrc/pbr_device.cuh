@@ -121,11 +121,13 @@ __device__ __forceinline__ float4 make_edge(float xa, float ya, float xb, float 
   return make_float4(A, B, xf, yf);
 }
 
+// Triangle setup from screen-space vertices (to_screen of the clip
+// coordinates).  Returns 1 when the triangle is kept (and, if WRITE, its
+// records are written at slot), 0 when it is culled or covers no pixel centre.
 template <bool WRITE>
-__device__ __forceinline__ int setup_tri(const SceneParams& P, const SetupCtx& S, float4 c0, float4 n0, float4 c1,
-                                         float4 n1, float4 c2, float4 n2, int slot, float4 col, int draw_id,
-                                         bool smooth) {
-  SV v0 = to_screen(c0, S.W, S.H), v1 = to_screen(c1, S.W, S.H), v2 = to_screen(c2, S.W, S.H);
+__device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx& S, SV v0, float4 n0, SV v1,
+                                            float4 n1, SV v2, float4 n2, int slot, float4 col, int draw_id,
+                                            bool smooth) {
   float area2 = (v1.x - v0.x) * (v2.y - v0.y) - (v2.x - v0.x) * (v1.y - v0.y);
   if (S.cull) {
     if (!(area2 < 0.f)) return 0;  // back-facing, degenerate or NaN
@@ -170,6 +172,14 @@ __device__ __forceinline__ int setup_tri(const SceneParams& P, const SetupCtx& S
     S.S3[slot] = col;
   }
   return 1;
+}
+
+template <bool WRITE>
+__device__ __forceinline__ int setup_tri(const SceneParams& P, const SetupCtx& S, float4 c0, float4 n0, float4 c1,
+                                         float4 n1, float4 c2, float4 n2, int slot, float4 col, int draw_id,
+                                         bool smooth) {
+  const SV v0 = to_screen(c0, S.W, S.H), v1 = to_screen(c1, S.W, S.H), v2 = to_screen(c2, S.W, S.H);
+  return setup_tri_sv<WRITE>(P, S, v0, n0, v1, n1, v2, n2, slot, col, draw_id, smooth);
 }
 
 __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {

@@ -6,25 +6,28 @@
 // on a block barrier:
 //
 //   K1  the scene's instances of every node, flattened in draw order into one
-//       table (lane = instance): model matrix M = [R(hpr)*s | t] and colour;
-//       then lane = vertex: clip = VP * M * v, n = normalize(mat3(M) n)
-//       (shaders/basic.vert:29-53)
+//       table (lane = instance, so all pose loads are in flight together):
+//       model matrix M = [R(hpr)*s | t] and colour; then lane = vertex:
+//       clip = VP * M * v, n = normalize(mat3(M) n)  (shaders/basic.vert:29-53)
 //   K2  lane = triangle: near clip, cull, watertight edges, depth plane, flat
 //       shading; compacted in draw order with a warp prefix sum (__shfl_up);
 //       then the warp-ballot binner: for each 32x16-pixel bin one
 //       __ballot_sync over the lanes (= triangles) is the bin's mask
-//   K3  per bin: an empty bin is written as background with 128-bit stores;
-//       otherwise the warp walks the bin's triangles in draw order and, per
-//       triangle, maps its bbox-in-bin pixels onto the lanes (edge test,
-//       strict-less depth test, colour of basic.frag:20-39) against a per-warp
-//       shared-memory depth/colour tile; then each lane owns one 16-pixel row
-//       segment, transposes RGBA to planes with byte permutes and stores
-//       each channel with one st.global.v4.
+//   K3  per bin: an empty bin is written as background with 128-bit stores.
+//       Otherwise the bin's candidate triangles and the pixels of their
+//       bbox-in-bin are laid out end to end (warp prefix sum of the areas) and
+//       dealt 32 per pass to the lanes, so many tiny triangles share a pass.
+//       Each covered pixel does a 64-bit atomicMin of (window depth, draw
+//       order + 1) into a shared-memory tile: strict-less depth with ties to
+//       the earlier draw, independent of lane order.  Then every lane resolves
+//       its own 16-pixel row segment (shaders/basic.frag:20-39, once per
+//       pixel), transposes RGBA to planes with byte permutes and stores each
+//       channel with one st.global.v4.
 //
 // Shared memory per warp: the triangle list plus one region that holds the
-// vertex cache / instance table during K1-K2 and the bin's depth / colour /
-// winner tile during K3.  The host picks this kernel when a scene has at most
-// 64 source triangles, 32 instances and 256 vertices, and W % 16 == 0.
+// vertex cache / instance table during K1-K2 and the bin's key tile during K3.
+// The host picks this kernel when a scene has at most 64 source triangles,
+// 32 instances and 256 vertices, and W % 16 == 0.
 #include "pbr_device.cuh"
 #include "pbr_launch.h"
 
@@ -33,14 +36,24 @@ namespace pbr {
 constexpr int kBinW = 32;  // bin = 32 x 16 pixels = 32 lanes x 16-pixel row segments
 constexpr int kBinH = 16;
 constexpr int kBinPx = kBinW * kBinH;
+constexpr int kWarps = 4;   // warps per block
+constexpr int kBlocksPerSm = 7;
 
 struct SmallLayout {
-  int t0, t1, t2, t3, t4, s0, s1, s2, s3, masks, vp, uni;
-  int vcache, itab;          // inside uni (setup)
-  int zbuf, cbuf, wbuf;      // inside uni (raster)
+  int t0, t1, t2, t3, bgrec, t4, s0, s1, s2, s3, masks, vp, uni;
+  int vcache, itab;  // inside uni (setup)
+  int keys;          // inside uni (raster): uint64 [16][32]
   int per_warp;
 };
 
+// Per-warp shared memory.  Triangle records T0..T4 (and S0..S3 for smooth
+// shading); bgrec is a T4-shaped record just before T4[0] holding the
+// background colour (.z) and winner -1 (.w), so that draw order + 1 indexes
+// both.  The setup stage's vertex cache (3 float4 per vertex: clip position;
+// normal with .w = z + w; screen position), instance table (5 float4 per
+// instance: 3 model-matrix rows, colour, meta) and view-projection matrix
+// share one region with the raster stage's key tile.  Cartpole-sized scenes
+// need 8064 bytes a warp, which keeps 7 blocks of 4 warps on an SM.
 __host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int icap, int nbins, int smooth) {
   SmallLayout L;
   int off = 0;
@@ -49,6 +62,7 @@ __host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int i
   L.t1 = off; off += align16(t4);
   L.t2 = off; off += align16(t4);
   L.t3 = off; off += align16(t4);
+  L.bgrec = off; off += 16;
   L.t4 = off; off += align16(t4);
   if (smooth) {
     L.s0 = off; off += align16(t4);
@@ -58,16 +72,14 @@ __host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int i
   } else {
     L.s0 = L.s1 = L.s2 = L.s3 = 0;
   }
-  L.masks = off; off += align16(nbins * (tri_cap / 32) * 4);
-  L.vp = off; off += 64;
+  L.masks = off; off += align16(nbins * ((tri_cap + 31) / 32) * 4);
   L.uni = off;
-  const int setup = align16(vcap * 32) + align16(icap * 80);
-  const int raster = kBinPx * 4 + kBinPx * 4 + kBinPx;
+  const int setup = align16(vcap * 48) + align16(icap * 80) + 64;
+  const int raster = kBinPx * 8;
   L.vcache = off;
-  L.itab = off + align16(vcap * 32);
-  L.zbuf = off;
-  L.cbuf = off + kBinPx * 4;
-  L.wbuf = off + kBinPx * 8;
+  L.itab = off + align16(vcap * 48);
+  L.vp = L.itab + align16(icap * 80);
+  L.keys = off;
   off += align16(setup > raster ? setup : raster);
   L.per_warp = align16(off);
   return L;
@@ -75,6 +87,7 @@ __host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int i
 
 int small_smem_per_warp(const RasterArgs& A, int W, int H) {
   const int nbins = ((W + kBinW - 1) / kBinW) * ((H + kBinH - 1) / kBinH);
+  if (nbins > 64) return -1;  // the non-empty bins of a scene are one 64-bit mask
   return small_layout(A.tri_cap, A.vcap, A.icap, nbins, A.smooth_any).per_warp;
 }
 
@@ -89,16 +102,62 @@ __device__ __forceinline__ void rgba_to_planes(uint32_t p0, uint32_t p1, uint32_
   a = __byte_perm(t2, t3, 0x7632);
 }
 
-template <int WARPS, bool PLAIN, bool WINNER>
-__global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) small_kernel(const __grid_constant__ SceneParams P,
-                                                                          const __grid_constant__ RasterArgs A) {
+__device__ __forceinline__ int node_count(const NodeDesc& nd, int k) {
+  const int c = nd.counts ? nd.counts[k] : nd.ips;
+  return max(0, min(c, nd.ips));
+}
+
+// Triangle t of the flattened scene: count (WRITE = false) or set up at slot.
+// Smooth meshes take the vertex normals from the vertex cache; a flat mesh's
+// triangle is lit with its first vertex's normal (all three are identical),
+// transformed here, only for triangles that survive culling.
+template <bool WRITE, bool SMOOTH>
+__device__ __forceinline__ int small_tri(const SceneParams& P, const SetupCtx& S, const float4* vcache,
+                                         const float4* itab, int total_inst, int t, int slot) {
+  int inst = 0;
+  while (inst + 1 < total_inst && __float_as_int(itab[(inst + 1) * 5 + 4].w) <= t) ++inst;
+  const float4 meta = itab[inst * 5 + 4];
+  const MeshDesc& me = P.meshes[P.nodes[__float_as_int(meta.x)].mesh];
+  const int ti = t - __float_as_int(meta.w);
+  const int vbase = __float_as_int(meta.y);
+  const int i0 = me.idx[3 * ti], i1 = me.idx[3 * ti + 1], i2 = me.idx[3 * ti + 2];
+  float4 n0 = vcache[3 * (vbase + i0) + 1], n1 = vcache[3 * (vbase + i1) + 1], n2 = vcache[3 * (vbase + i2) + 1];
+  const bool front = n0.w >= 0.f && n1.w >= 0.f && n2.w >= 0.f;
+  if (!front && n0.w < 0.f && n1.w < 0.f && n2.w < 0.f) return 0;
+  const float4 col = itab[inst * 5 + 3];
+  const int draw_id = __float_as_int(meta.z) + ti;
+  const bool smooth = SMOOTH && me.smooth != 0;
+  if (WRITE && !SMOOTH) {
+    const float4 r0 = itab[inst * 5 + 0], r1 = itab[inst * 5 + 1], r2 = itab[inst * 5 + 2];
+    const float ax = me.nrm[3 * i0], ay = me.nrm[3 * i0 + 1], az = me.nrm[3 * i0 + 2];
+    const float nx = r0.x * ax + r0.y * ay + r0.z * az;
+    const float ny = r1.x * ax + r1.y * ay + r1.z * az;
+    const float nz = r2.x * ax + r2.y * ay + r2.z * az;
+    const float l2 = nx * nx + ny * ny + nz * nz;
+    const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
+    n0 = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
+    n1 = n0;
+    n2 = n0;
+  }
+  if (front) {
+    const float4 a = vcache[3 * (vbase + i0) + 2], b = vcache[3 * (vbase + i1) + 2], c = vcache[3 * (vbase + i2) + 2];
+    return setup_tri_sv<WRITE>(P, S, SV{a.x, a.y, a.z, a.w}, n0, SV{b.x, b.y, b.z, b.w}, n1, SV{c.x, c.y, c.z, c.w},
+                               n2, slot, col, draw_id, smooth);
+  }
+  return clip_tri<WRITE>(P, S, vcache[3 * (vbase + i0)], n0, vcache[3 * (vbase + i1)], n1, vcache[3 * (vbase + i2)],
+                         n2, i0, i1, i2, slot, col, draw_id, smooth);
+}
+
+template <bool PLAIN, bool WINNER, bool SMOOTH>
+__global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const __grid_constant__ SceneParams P,
+                                                                         const __grid_constant__ RasterArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int W = P.W, H = P.H, HW = W * H;
+  const int W = P.W, H = P.H, HW = W * H, C = P.C;
   const int bins_x = (W + kBinW - 1) / kBinW, bins_y = (H + kBinH - 1) / kBinH;
   const int nbins = bins_x * bins_y;
-  const int words = A.tri_cap >> 5;
-  const SmallLayout L = small_layout(A.tri_cap, A.vcap, A.icap, nbins, A.smooth_any);
+  const int words = (A.tri_cap + 31) >> 5;
+  const SmallLayout L = small_layout(A.tri_cap, A.vcap, A.icap, nbins, SMOOTH ? 1 : 0);
   unsigned char* base = smem + warp * L.per_warp;
   SetupCtx S;
   S.T0 = reinterpret_cast<float4*>(base + L.t0);
@@ -118,51 +177,63 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) small_kernel(const __g
   uint32_t* masks = reinterpret_cast<uint32_t*>(base + L.masks);
   float* s_vp = reinterpret_cast<float*>(base + L.vp);
   float4* vcache = reinterpret_cast<float4*>(base + L.vcache);
-  float4* itab = reinterpret_cast<float4*>(base + L.itab);  // per instance: 3 matrix rows, colour, meta
-  float* zb = reinterpret_cast<float*>(base + L.zbuf);       // [16][32]: pixel j of lane l at j*32 + l
-  uint32_t* cb = reinterpret_cast<uint32_t*>(base + L.cbuf);
-  uint8_t* wb = base + L.wbuf;
+  float4* itab = reinterpret_cast<float4*>(base + L.itab);
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(base + L.keys);  // [16][32]
+  // T4 record r - 1 for r = draw order + 1 (r = 0: the background record)
+  const unsigned char* rec4 = base + L.bgrec;
 
-  const int seg_r = lane >> 1, seg_x = (lane & 1) * 16;
   const uint32_t bg = P.bg_packed;
-  uint32_t bgw[4];
-#pragma unroll
-  for (int c = 0; c < 4; ++c) bgw[c] = ((bg >> (8 * c)) & 0xffu) * 0x01010101u;
+  if (lane == 0) *reinterpret_cast<float4*>(base + L.bgrec) = make_float4(0.f, 0.f, __uint_as_float(bg), __int_as_float(-1));
+  const uint32_t bg0 = (bg & 0xffu) * 0x01010101u, bg1 = ((bg >> 8) & 0xffu) * 0x01010101u;
+  const uint32_t bg2 = ((bg >> 16) & 0xffu) * 0x01010101u, bg3 = (bg >> 24) * 0x01010101u;
+  // this lane's 16-pixel row segment of a bin: row lane / 2, columns (lane % 2) * 16 .. + 15
+  const int seg_r = lane >> 1, seg_x = (lane & 1) * 16;
+  const int lane_off = seg_r * W + seg_x;
+  // key of an untouched pixel: depth 1.0 (the clear), draw order 0 (before every triangle)
+  const unsigned long long clear_key = (unsigned long long)__float_as_uint(1.f) << 32;
 
-  for (int k = blockIdx.x * WARPS + warp; k < P.N; k += gridDim.x * WARPS) {
+  for (int k = blockIdx.x * kWarps + warp; k < P.N; k += gridDim.x * kWarps) {
     if (lane < 16) s_vp[lane] = P.vp[(long long)k * 16 + lane];
 
     // ---- K1: instance table, flattened over nodes in draw order ---------
-    // node-level counts are uniform across the warp
     int total_inst = 0, total_verts = 0, total_tris = 0;
     for (int n = A.node_begin; n < A.node_end; ++n) {
       const NodeDesc& nd = P.nodes[n];
-      int cnt = nd.counts ? nd.counts[k] : nd.ips;
-      cnt = max(0, min(cnt, nd.ips));
+      const int cnt = node_count(nd, k);
       const MeshDesc& me = P.meshes[nd.mesh];
-      for (int i = lane; i < cnt; i += 32) {
-        const long long id = nd.shared ? (long long)i : (long long)k * nd.ips + i;
-        float m[12];
-        build_model(nd, id, m);
-        float4* e = itab + (total_inst + i) * 5;
-        e[0] = make_float4(m[0], m[1], m[2], m[3]);
-        e[1] = make_float4(m[4], m[5], m[6], m[7]);
-        e[2] = make_float4(m[8], m[9], m[10], m[11]);
-        const float4 cc = *reinterpret_cast<const float4*>(nd.color + id * 4);
-        e[3] = cc;
-        // meta: node, first vertex, draw id of triangle 0, first triangle
-        e[4] = make_float4(__int_as_float(n), __int_as_float(total_verts + i * me.nv),
-                           __int_as_float((nd.rank_base + i) * P.max_tris), __int_as_float(total_tris + i * me.nt));
-      }
       total_inst += cnt;
       total_verts += cnt * me.nv;
       total_tris += cnt * me.nt;
+    }
+    for (int i = lane; i < total_inst; i += 32) {
+      int n = A.node_begin, ai = 0, av = 0, at = 0;
+      for (; n < A.node_end; ++n) {
+        const int cnt = node_count(P.nodes[n], k);
+        if (i < ai + cnt) break;
+        const MeshDesc& me = P.meshes[P.nodes[n].mesh];
+        ai += cnt;
+        av += cnt * me.nv;
+        at += cnt * me.nt;
+      }
+      const NodeDesc& nd = P.nodes[n];
+      const MeshDesc& me = P.meshes[nd.mesh];
+      const int li = i - ai;
+      const long long id = nd.shared ? (long long)li : (long long)k * nd.ips + li;
+      float m[12];
+      build_model(nd, id, m);
+      float4* e = itab + i * 5;
+      e[0] = make_float4(m[0], m[1], m[2], m[3]);
+      e[1] = make_float4(m[4], m[5], m[6], m[7]);
+      e[2] = make_float4(m[8], m[9], m[10], m[11]);
+      e[3] = *reinterpret_cast<const float4*>(nd.color + id * 4);
+      // meta: node, first vertex, draw id of triangle 0, first triangle
+      e[4] = make_float4(__int_as_float(n), __int_as_float(av + li * me.nv),
+                         __int_as_float((nd.rank_base + li) * P.max_tris), __int_as_float(at + li * me.nt));
     }
     __syncwarp();
 
     // ---- K1: vertices ------------------------------------------------------
     for (int v = lane; v < total_verts; v += 32) {
-      // find the instance holding flat vertex v (instances are few: linear scan)
       int inst = 0;
       while (inst + 1 < total_inst && __float_as_int(itab[(inst + 1) * 5 + 4].y) <= v) ++inst;
       const float4 meta = itab[inst * 5 + 4];
@@ -180,14 +251,22 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) small_kernel(const __g
       c.y = q1.x * wx + q1.y * wy + q1.z * wz + q1.w;
       c.z = q2.x * wx + q2.y * wy + q2.z * wz + q2.w;
       c.w = q3.x * wx + q3.y * wy + q3.z * wz + q3.w;
-      const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
-      const float nx = r0.x * ax + r0.y * ay + r0.z * az;
-      const float ny = r1.x * ax + r1.y * ay + r1.z * az;
-      const float nz = r2.x * ax + r2.y * ay + r2.z * az;
-      const float l2 = nx * nx + ny * ny + nz * nz;
-      const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
-      vcache[2 * v] = c;
-      vcache[2 * v + 1] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
+      float4 nv = make_float4(0.f, 0.f, 0.f, c.z + c.w);
+      if (SMOOTH) {
+        const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
+        const float nx = r0.x * ax + r0.y * ay + r0.z * az;
+        const float ny = r1.x * ax + r1.y * ay + r1.z * az;
+        const float nz = r2.x * ax + r2.y * ay + r2.z * az;
+        const float l2 = nx * nx + ny * ny + nz * nz;
+        const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
+        nv.x = nx * inv;
+        nv.y = ny * inv;
+        nv.z = nz * inv;
+      }
+      const SV sv = to_screen(c, S.W, S.H);
+      vcache[3 * v] = c;
+      vcache[3 * v + 1] = nv;
+      vcache[3 * v + 2] = make_float4(sv.x, sv.y, sv.z, sv.iw);
     }
     __syncwarp();
 
@@ -195,25 +274,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) small_kernel(const __g
     int tri_count = 0;
     for (int t0 = 0; t0 < total_tris; t0 += 32) {
       const int t = t0 + lane;
-      int c = 0, inst = 0, ti = 0, vbase = 0, i0 = 0, i1 = 0, i2 = 0;
-      float4 col = make_float4(0.f, 0.f, 0.f, 0.f);
-      bool smooth = false;
-      int dbase = 0;
-      if (t < total_tris) {
-        // instance holding flat triangle t (instances are few: linear scan)
-        while (inst + 1 < total_inst && __float_as_int(itab[(inst + 1) * 5 + 4].w) <= t) ++inst;
-        const float4 meta = itab[inst * 5 + 4];
-        const MeshDesc& me = P.meshes[P.nodes[__float_as_int(meta.x)].mesh];
-        ti = t - __float_as_int(meta.w);
-        vbase = __float_as_int(meta.y);
-        dbase = __float_as_int(meta.z);
-        smooth = me.smooth != 0;
-        col = itab[inst * 5 + 3];
-        i0 = me.idx[3 * ti];
-        i1 = me.idx[3 * ti + 1];
-        i2 = me.idx[3 * ti + 2];
-        c = process_tri<false>(P, S, vcache, vbase, i0, i1, i2, 0, col, 0, smooth);
-      }
+      const int c = t < total_tris ? small_tri<false, SMOOTH>(P, S, vcache, itab, total_inst, t, 0) : 0;
       int incl = c;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -221,7 +282,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) small_kernel(const __g
         if (lane >= o) incl += y;
       }
       const int total = __shfl_sync(0xffffffffu, incl, 31);
-      if (c > 0) process_tri<true>(P, S, vcache, vbase, i0, i1, i2, tri_count + incl - c, col, dbase + ti, smooth);
+      if (c > 0) small_tri<true, SMOOTH>(P, S, vcache, itab, total_inst, t, tri_count + incl - c);
       tri_count += total;
     }
     __syncwarp();
@@ -229,6 +290,7 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) small_kernel(const __g
     // ---- warp-ballot binner ----------------------------------------------
     const int T = tri_count;
     const int nw = (T + 31) >> 5;
+    unsigned long long ne = 0ull;  // bit b: bin b has candidates
     for (int w = 0; w < nw; ++w) {
       const int t = w * 32 + lane;
       int bx0 = 1 << 20, bx1 = -1, by0 = 1 << 20, by1 = -1;
@@ -239,76 +301,114 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) small_kernel(const __g
         by0 = (int)(yb & 0xffffu) / kBinH;
         by1 = (int)(yb >> 16) / kBinH;
       }
-      for (int b = 0; b < nbins; ++b) {
-        const int by = b / bins_x, bx = b - by * bins_x;
-        const uint32_t m = __ballot_sync(0xffffffffu, (bx >= bx0) && (bx <= bx1) && (by >= by0) && (by <= by1));
-        if (lane == 0) masks[b * words + w] = m;
+      int b = 0;
+      for (int by = 0; by < bins_y; ++by) {
+        const bool yin = (by >= by0) && (by <= by1);
+        for (int bx = 0; bx < bins_x; ++bx, ++b) {
+          const uint32_t m = __ballot_sync(0xffffffffu, yin && (bx >= bx0) && (bx <= bx1));
+          if (lane == 0) masks[b * words + w] = m;
+          ne |= (unsigned long long)(m != 0u) << b;
+        }
       }
     }
     __syncwarp();
 
-    // ---- K3: bin by bin ----------------------------------------------------
-    for (int b = 0; b < nbins; ++b) {
-      const int by = b / bins_x, bx = b - by * bins_x;
-      const int row0 = by * kBinH, col0 = bx * kBinW;
-      const int y = row0 + seg_r, x0 = col0 + seg_x;
-      const bool active = (y < H) && (x0 < W);
-      const long long pix0 = (long long)k * HW + (long long)y * W + x0;
-      uint8_t* out0 = A.out + (long long)k * P.C * HW + (long long)y * W + x0;
-      uint32_t any = 0u;
-      for (int w = 0; w < nw; ++w) any |= masks[b * words + w];
-      if (any == 0u) {
-        if (!PLAIN && active) {
-          for (int c = 0; c < P.C; ++c)
-            *reinterpret_cast<uint4*>(out0 + (long long)c * HW) = make_uint4(bgw[c], bgw[c], bgw[c], bgw[c]);
-          if (A.depth) {
-            float4* d = reinterpret_cast<float4*>(A.depth + pix0);
-            const float4 one = make_float4(1.f, 1.f, 1.f, 1.f);
-            d[0] = one; d[1] = one; d[2] = one; d[3] = one;
-          }
-          if (WINNER) {
-            int4* d = reinterpret_cast<int4*>(A.winner + pix0);
-            const int4 none = make_int4(-1, -1, -1, -1);
-            d[0] = none; d[1] = none; d[2] = none; d[3] = none;
-          }
+    // ---- K3: background, then the bins that have candidates ---------------
+    uint8_t* const lane_out = A.out + (size_t)k * C * HW + lane_off;
+    const size_t lane_pix = (size_t)k * HW + lane_off;
+    if (!PLAIN) {
+      // the whole scene as background: coalesced 512-byte warp stores, four per trip
+      const int n16 = HW >> 4;  // uint4 per plane (HW % 16 == 0)
+      uint4* p = reinterpret_cast<uint4*>(A.out + (size_t)k * C * HW);
+      for (int c = 0; c < C; ++c, p += n16) {
+        const uint32_t v = c == 0 ? bg0 : (c == 1 ? bg1 : (c == 2 ? bg2 : bg3));
+        const uint4 v4 = make_uint4(v, v, v, v);
+        int i = lane;
+        for (; i + 96 < n16; i += 128) {
+          p[i] = v4;
+          p[i + 32] = v4;
+          p[i + 64] = v4;
+          p[i + 96] = v4;
         }
-        continue;
+        for (; i < n16; i += 32) p[i] = v4;
       }
-      // this bin's depth / colour / winner tile
+      if (A.depth || WINNER) {
+        for (int p = lane * 4; p < HW; p += 128) {
+          if (A.depth) *reinterpret_cast<float4*>(A.depth + (size_t)k * HW + p) = make_float4(1.f, 1.f, 1.f, 1.f);
+          if (WINNER) *reinterpret_cast<int4*>(A.winner + (size_t)k * HW + p) = make_int4(-1, -1, -1, -1);
+        }
+      }
+    }
+    for (unsigned long long rem = ne; rem != 0ull; rem &= rem - 1ull) {
+      const int b = __ffsll((long long)rem) - 1;
+      const int by = b / bins_x;
+      const int row0 = by * kBinH, col0 = (b - by * bins_x) * kBinW;
+      {
+        const bool active = (row0 + seg_r < H) && (col0 + seg_x < W);
+        const int boff = row0 * W + col0;
+        // key tile: depth bits << 32 | (draw order + 1); order 0 = the buffer's previous content
+        if (PLAIN) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        float z0 = 1.f;
-        uint32_t c0 = bg;
-        if (PLAIN && active) {
-          z0 = A.zbuf[pix0 + j];
-          c0 = A.cbuf[pix0 + j];
+          for (int j = 0; j < 16; ++j) {
+            unsigned long long k0 = clear_key;
+            if (active) k0 = (unsigned long long)(__float_as_uint(A.zbuf[lane_pix + boff + j]) & 0x7fffffffu) << 32;
+            keys[j * 32 + lane] = k0;
+          }
+        } else {
+          const uint4 ck = make_uint4(0u, __float_as_uint(1.f), 0u, __float_as_uint(1.f));
+#pragma unroll
+          for (int j = 0; j < 8; ++j) reinterpret_cast<uint4*>(keys)[j * 32 + lane] = ck;
         }
-        zb[j * 32 + lane] = z0;
-        cb[j * 32 + lane] = c0;
-        if (WINNER) wb[j * 32 + lane] = 0xffu;
-      }
-      __syncwarp();
-      for (int w = 0; w < nw; ++w) {
-        uint32_t m = masks[b * words + w];
-        while (m) {
-          const int t = w * 32 + __ffs(m) - 1;
-          m &= m - 1u;
-          const float4 zp = S.T3[t];
-          const float4 meta = S.T4[t];
-          const uint32_t xb = __float_as_uint(zp.w), yb = __float_as_uint(meta.x);
-          const int ax0 = max((int)(xb & 0xffffu), col0), ax1 = min((int)(xb >> 16), col0 + kBinW - 1);
-          const int ay0 = max((int)(yb & 0xffffu), row0), ay1 = min((int)(yb >> 16), row0 + kBinH - 1);
-          const int bw = ax1 - ax0 + 1, bh = ay1 - ay0 + 1;
-          if (bw <= 0 || bh <= 0) continue;
-          const float4 e0 = S.T0[t], e1 = S.T1[t], e2 = S.T2[t];
-          const uint32_t fl = __float_as_uint(meta.y);
-          const uint32_t flat_col = __float_as_uint(meta.z);
-          const float inv_bw = 1.f / (float)bw;
-          const int npx = bw * bh;
-          for (int i = lane; i < npx; i += 32) {
-            const int ry = (int)(((float)i + 0.5f) * inv_bw);
-            const int xx = ax0 + i - ry * bw, yy = ay0 + ry;
+        __syncwarp();
+        for (int w = 0; w < nw; ++w) {
+          const uint32_t m = masks[b * words + w];
+          if (m == 0u) continue;
+          // this lane's candidate (triangle w*32+lane if its bit is set) and its bbox-in-bin
+          int ax0 = 0, ay0 = 0, bw = 1, npx = 0;
+          if ((m >> lane) & 1u) {
+            const int t = w * 32 + lane;
+            const uint32_t xb = __float_as_uint(S.T3[t].w), yb = __float_as_uint(S.T4[t].x);
+            ax0 = max((int)(xb & 0xffffu), col0);
+            const int ax1 = min((int)(xb >> 16), col0 + kBinW - 1);
+            ay0 = max((int)(yb & 0xffffu), row0);
+            const int ay1 = min((int)(yb >> 16), row0 + kBinH - 1);
+            const int bh = ay1 - ay0 + 1;
+            bw = ax1 - ax0 + 1;
+            npx = (bw > 0 && bh > 0) ? bw * bh : 0;
+            bw = max(bw, 1);
+          }
+          const float ibw = __fdividef(1.f, (float)bw);
+          int incl = npx;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+          }
+          const int total = __shfl_sync(0xffffffffu, incl, 31);
+          for (int g0 = 0; g0 < total; g0 += 32) {
+            const int g = g0 + lane;
+            // owner lane: the first lane whose inclusive area sum exceeds g
+            int o = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+              const int probe = __shfl_sync(0xffffffffu, incl, o + step - 1);
+              if (probe <= g) o += step;
+            }
+            const int o_start = __shfl_sync(0xffffffffu, incl - npx, o);
+            const int o_ax0 = __shfl_sync(0xffffffffu, ax0, o);
+            const int o_ay0 = __shfl_sync(0xffffffffu, ay0, o);
+            const int o_bw = __shfl_sync(0xffffffffu, bw, o);
+            const float o_ibw = __shfl_sync(0xffffffffu, ibw, o);
+            if (g >= total) continue;
+            const int t = w * 32 + o;
+            const int local = g - o_start;
+            // row within the bbox: (local + 0.5) / bw lies at least 0.5 / bw >= 1/64 from an
+            // integer, far more than the error of the approximate reciprocal product
+            const int ry = (int)(((float)local + 0.5f) * o_ibw);
+            const int xx = o_ax0 + local - ry * o_bw, yy = o_ay0 + ry;
             const float px = (float)xx + 0.5f, py = (float)yy + 0.5f;
+            const float4 e0 = S.T0[t], e1 = S.T1[t], e2 = S.T2[t], zp = S.T3[t];
+            const uint32_t fl = __float_as_uint(S.T4[t].y);
             const float E0 = fmaf(e0.x, px - e0.z, e0.y * (py - e0.w));
             const float E1 = fmaf(e1.x, px - e1.z, e1.y * (py - e1.w));
             const float E2 = fmaf(e2.x, px - e2.z, e2.y * (py - e2.w));
@@ -318,97 +418,109 @@ __global__ void __launch_bounds__(WARPS * 32, 24 / WARPS) small_kernel(const __g
             if (in0 && in1 && in2) {
               const float z = fmaxf(fmaf(zp.x, px, fmaf(zp.y, py, zp.z)), 0.f);
               const int p = (yy - row0) * kBinW + (xx - col0);
-              const int idx = (p & 15) * 32 + (p >> 4);
-              if (z < zb[idx]) {
-                zb[idx] = z;
-                cb[idx] = (fl & 8u) ? shade_smooth(P, S, t, px, py) : flat_col;
-                if (WINNER) wb[idx] = (uint8_t)t;
-              }
+              // z >= 0, so its bits order like the values (the mask folds -0 into +0)
+              const unsigned long long key =
+                  ((unsigned long long)(__float_as_uint(z) & 0x7fffffffu) << 32) | (unsigned)(t + 1);
+              atomicMin(&keys[(p & 15) * 32 + (p >> 4)], key);
             }
           }
-          __syncwarp();
         }
-      }
-      // each lane stores its 16-pixel row segment
-      if (active) {
-        if (PLAIN) {
-          uint4* cd = reinterpret_cast<uint4*>(A.cbuf + pix0);
-          float4* zd = reinterpret_cast<float4*>(A.zbuf + pix0);
-#pragma unroll
-          for (int g = 0; g < 4; ++g) {
-            cd[g] = make_uint4(cb[(4 * g) * 32 + lane], cb[(4 * g + 1) * 32 + lane], cb[(4 * g + 2) * 32 + lane],
-                               cb[(4 * g + 3) * 32 + lane]);
-            zd[g] = make_float4(zb[(4 * g) * 32 + lane], zb[(4 * g + 1) * 32 + lane], zb[(4 * g + 2) * 32 + lane],
-                                zb[(4 * g + 3) * 32 + lane]);
-          }
-        } else {
+        __syncwarp();
+        // resolve this lane's 16-pixel row segment, four pixels at a time
+        if (active) {
+          const uint32_t* klo = reinterpret_cast<const uint32_t*>(keys) + 2 * lane;  // low word of key j: klo[64 j]
           uint32_t pr[4], pg[4], pb[4], pa[4];
 #pragma unroll
-          for (int g = 0; g < 4; ++g)
-            rgba_to_planes(cb[(4 * g) * 32 + lane], cb[(4 * g + 1) * 32 + lane], cb[(4 * g + 2) * 32 + lane],
-                           cb[(4 * g + 3) * 32 + lane], pr[g], pg[g], pb[g], pa[g]);
-          *reinterpret_cast<uint4*>(out0) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
-          if (P.C > 1) *reinterpret_cast<uint4*>(out0 + HW) = make_uint4(pg[0], pg[1], pg[2], pg[3]);
-          if (P.C > 2) *reinterpret_cast<uint4*>(out0 + 2LL * HW) = make_uint4(pb[0], pb[1], pb[2], pb[3]);
-          if (P.C > 3) *reinterpret_cast<uint4*>(out0 + 3LL * HW) = make_uint4(pa[0], pa[1], pa[2], pa[3]);
-          if (A.depth) {
-            float4* d = reinterpret_cast<float4*>(A.depth + pix0);
+          for (int g = 0; g < 4; ++g) {
+            uint32_t col[4];
 #pragma unroll
-            for (int g = 0; g < 4; ++g)
-              d[g] = make_float4(zb[(4 * g) * 32 + lane], zb[(4 * g + 1) * 32 + lane], zb[(4 * g + 2) * 32 + lane],
-                                 zb[(4 * g + 3) * 32 + lane]);
+            for (int q = 0; q < 4; ++q) {
+              const int j = 4 * g + q;
+              const uint32_t r = klo[64 * j];
+              const float4* rec = reinterpret_cast<const float4*>(rec4 + 16 * r);
+              if (PLAIN) {
+                col[q] = r ? __float_as_uint(rec->z) : A.cbuf[lane_pix + boff + j];
+              } else if (SMOOTH && (__float_as_uint(rec->y) & 8u)) {
+                col[q] = shade_smooth(P, S, (int)r - 1, (float)(col0 + seg_x + j) + 0.5f, (float)(row0 + seg_r) + 0.5f);
+              } else {
+                col[q] = __float_as_uint(rec->z);
+              }
+            }
+            if (PLAIN) {
+              reinterpret_cast<uint4*>(A.cbuf + lane_pix + boff)[g] = make_uint4(col[0], col[1], col[2], col[3]);
+            } else {
+              rgba_to_planes(col[0], col[1], col[2], col[3], pr[g], pg[g], pb[g], pa[g]);
+            }
+          }
+          if (PLAIN || A.depth) {
+            float4* zd = reinterpret_cast<float4*>((PLAIN ? A.zbuf : A.depth) + lane_pix + boff);
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+              float z4[4];
+#pragma unroll
+              for (int q = 0; q < 4; ++q) z4[q] = __uint_as_float(klo[64 * (4 * g + q) + 1]);
+              zd[g] = make_float4(z4[0], z4[1], z4[2], z4[3]);
+            }
+          }
+          if (!PLAIN) {
+            uint8_t* o = lane_out + boff;
+            *reinterpret_cast<uint4*>(o) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
+            if (C > 1) *reinterpret_cast<uint4*>(o + HW) = make_uint4(pg[0], pg[1], pg[2], pg[3]);
+            if (C > 2) *reinterpret_cast<uint4*>(o + 2 * HW) = make_uint4(pb[0], pb[1], pb[2], pb[3]);
+            if (C > 3) *reinterpret_cast<uint4*>(o + 3 * HW) = make_uint4(pa[0], pa[1], pa[2], pa[3]);
           }
           if (WINNER) {
-            int wi[16];
+            int4* d = reinterpret_cast<int4*>(A.winner + lane_pix + boff);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int t = wb[j * 32 + lane];
-              wi[j] = (t != 0xff) ? __float_as_int(S.T4[t].w) : -1;
+            for (int g = 0; g < 4; ++g) {
+              int wi[4];
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                wi[q] = __float_as_int(reinterpret_cast<const float4*>(rec4 + 16 * klo[64 * (4 * g + q)])->w);
+              d[g] = make_int4(wi[0], wi[1], wi[2], wi[3]);
             }
-            int4* d = reinterpret_cast<int4*>(A.winner + pix0);
-#pragma unroll
-            for (int g = 0; g < 4; ++g) d[g] = make_int4(wi[4 * g], wi[4 * g + 1], wi[4 * g + 2], wi[4 * g + 3]);
           }
         }
+        __syncwarp();
       }
-      __syncwarp();
     }
-    __syncwarp();  // the next scene's K1 reuses the raster tile as vertex cache
+    __syncwarp();  // the next scene's K1 reuses the key tile as vertex cache
   }
 }
 
 // ---------------------------------------------------------------------------
 
-template <int WP, bool PL, bool WN>
+template <bool PL, bool WN, bool SM>
 static const void* small_fn() {
-  return reinterpret_cast<const void*>(&small_kernel<WP, PL, WN>);
+  return reinterpret_cast<const void*>(&small_kernel<PL, WN, SM>);
 }
 
-static const void* pick_small(int warps, bool plain, bool winner) {
+static const void* pick_small(bool plain, bool winner, bool smooth) {
   if (plain && winner) return nullptr;
-  if (warps == 4) return plain ? small_fn<4, true, false>() : (winner ? small_fn<4, false, true>() : small_fn<4, false, false>());
-  if (warps == 8) return plain ? small_fn<8, true, false>() : (winner ? small_fn<8, false, true>() : small_fn<8, false, false>());
-  return nullptr;
+  if (smooth) return plain ? small_fn<true, false, true>() : (winner ? small_fn<false, true, true>() : small_fn<false, false, true>());
+  return plain ? small_fn<true, false, false>() : (winner ? small_fn<false, true, false>() : small_fn<false, false, false>());
 }
 
-cudaError_t small_set_smem_limit(int warps, bool plain, bool winner, int bytes) {
-  const void* f = pick_small(warps, plain, winner);
+int small_warps() { return kWarps; }
+
+cudaError_t small_set_smem_limit(bool plain, bool winner, bool smooth, int bytes) {
+  const void* f = pick_small(plain, winner, smooth);
   if (!f) return cudaErrorInvalidValue;
   return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-cudaError_t small_occupancy(int warps, bool plain, bool winner, int smem_bytes, int* blocks_per_sm) {
-  const void* f = pick_small(warps, plain, winner);
+cudaError_t small_occupancy(bool plain, bool winner, bool smooth, int smem_bytes, int* blocks_per_sm) {
+  const void* f = pick_small(plain, winner, smooth);
   if (!f) return cudaErrorInvalidValue;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, warps * 32, smem_bytes);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, kWarps * 32, smem_bytes);
 }
 
-cudaError_t small_launch(int warps, bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int grid,
-                         int smem_bytes, cudaStream_t stream) {
-  const void* f = pick_small(warps, plain, winner);
+cudaError_t small_launch(bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int grid, int smem_bytes,
+                         cudaStream_t stream) {
+  const void* f = pick_small(plain, winner, A.smooth_any != 0);
   if (!f) return cudaErrorInvalidValue;
   void* args[] = {const_cast<SceneParams*>(&P), const_cast<RasterArgs*>(&A)};
-  return cudaLaunchKernel(f, dim3(grid), dim3(warps * 32), args, (size_t)smem_bytes, stream);
+  return cudaLaunchKernel(f, dim3(grid), dim3(kWarps * 32), args, (size_t)smem_bytes, stream);
 }
 
 }  // namespace pbr

@@ -68,10 +68,11 @@ struct SoftCtx {
 // front of the near plane are dropped), back faces culled, bbox widened by
 // the coverage cutoff.  Records:
 //   R0..R2  edge k: (A, B, x_ref, y_ref)      R3 (1/L0, 1/L1, 1/L2, area2)
-//   R4      (iw0, iw1, iw2, x-box)            R5 (y-box, flags, instance slot, -)
+//   R4      (iw0, iw1, iw2, x-box)            R5 (y-box, flags, instance slot, d2)
 //   R6      instance colour                   R7..R9 (n_k, flat shaded colour channel k)
 //   R10..R12 (clip x, clip y, clip w, mesh vertex index) of vertex k
-//   R13, R14 screen vertices (x0, y0, x1, y1), (x2, y2, -, -)
+//   R13, R14 screen vertices (x0, y0, x1, y1), (x2, y2, d0, d1); R5.w = d2, where
+//            d_k = w_k - w_ref is vertex k's depth offset from the scene reference
 template <bool WRITE>
 __device__ __forceinline__ int soft_setup(const SceneParams& P, const SoftCtx& S, float4 c0, float4 n0, int v0,
                                           float4 c1, float4 n1, int v1, float4 c2, float4 n2, int v2, int slot,
@@ -103,7 +104,7 @@ __device__ __forceinline__ int soft_setup(const SceneParams& P, const SoftCtx& S
                              1.f / sqrtf(e2.x * e2.x + e2.y * e2.y), area2);
   const uint32_t xbox = (uint32_t)fx0 | ((uint32_t)fx1 << 16), ybox = (uint32_t)fy0 | ((uint32_t)fy1 << 16);
   S.R[4][slot] = make_float4(s0.iw, s1.iw, s2.iw, __uint_as_float(xbox));
-  S.R[5][slot] = make_float4(__uint_as_float(ybox), __uint_as_float(smooth ? 8u : 0u), __int_as_float(inst_slot), 0.f);
+  S.R[5][slot] = make_float4(__uint_as_float(ybox), __uint_as_float(smooth ? 8u : 0u), __int_as_float(inst_slot), n2.w);
   S.R[6][slot] = col;
   float rgb[3] = {0.f, 0.f, 0.f};
   if (!smooth) shade_rgb(P, n0.x, n0.y, n0.z, col, rgb);
@@ -114,7 +115,7 @@ __device__ __forceinline__ int soft_setup(const SceneParams& P, const SoftCtx& S
   S.R[11][slot] = make_float4(c1.x, c1.y, c1.w, __int_as_float(v1));
   S.R[12][slot] = make_float4(c2.x, c2.y, c2.w, __int_as_float(v2));
   S.R[13][slot] = make_float4(s0.x, s0.y, s1.x, s1.y);
-  S.R[14][slot] = make_float4(s2.x, s2.y, 0.f, 0.f);
+  S.R[14][slot] = make_float4(s2.x, s2.y, n0.w, n1.w);
   return 1;
 }
 
@@ -230,7 +231,14 @@ __device__ __forceinline__ bool soft_frag(const SceneParams& P, const SoftCtx& S
   f.D = f.Ds * T;
   if (!(f.D > 0.f)) return false;
   f.w = il.w / f.Q;
-  f.zs = (P.zfar - f.w) * inv_zr;
+  // normalised depth relative to the scene reference: zs - (zfar - w_ref)/(zfar - znear).  The softmax only
+  // sees differences, and this form keeps ~7 significant digits of them where (zfar - w) / (zfar - znear)
+  // would keep ~1 after the 1/gamma amplification
+  {
+    const float4 r14 = S.R[14][t];
+    const float d2 = S.R[5][t].w;
+    f.zs = -((f.E[0] * iw.x * r14.z + f.E[1] * iw.y * r14.w + f.E[2] * iw.z * d2) / f.Q) * inv_zr;
+  }
   const float4 n0 = S.R[7][t], n1 = S.R[8][t], n2 = S.R[9][t];
   const float4 col = S.R[6][t];
   const uint32_t fl = __float_as_uint(S.R[5][t].y);
@@ -718,7 +726,10 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
           const float l2 = nx * nx + ny * ny + nz * nz;
           const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
           vcache[2 * v] = c;
-          vcache[2 * v + 1] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
+          // depth offset from the scene reference w_ref = VP[15] (clip w of the world origin), computed
+          // without the large constant term so that it keeps its relative precision
+          const float dw = s_vp[12] * wx + s_vp[13] * wy + s_vp[14] * wz;
+          vcache[2 * v + 1] = make_float4(nx * inv, ny * inv, nz * inv, dw);
         }
         __syncthreads();
         const int total_t = nbc * nt;

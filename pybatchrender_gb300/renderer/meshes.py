@@ -29,8 +29,8 @@ class Mesh:
 
     positions: ``[nv,3]`` float32, normals: ``[nv,3]`` float32 (unit length),
     indices: ``[nt,3]`` int32, counter-clockwise when seen from the outside.
-    ``smooth`` is False when every triangle's three vertex normals are equal
-    (flat shading); the kernels use it only as a hint.
+    ``smooth`` is False when every triangle's three vertex normals are
+    identical (flat shading: a triangle is lit with its first vertex's normal).
     """
 
     positions: np.ndarray
@@ -48,7 +48,7 @@ class Mesh:
         if self.indices.size and (self.indices.min() < 0 or self.indices.max() >= len(self.positions)):
             raise ValueError("mesh indices out of range")
         tri_n = self.normals[self.indices]  # [nt,3,3]
-        self.smooth = bool(np.any(np.abs(tri_n - tri_n[:, :1, :]) > 1e-7))
+        self.smooth = bool(np.any(tri_n != tri_n[:, :1, :]))
 
     @property
     def num_vertices(self) -> int:

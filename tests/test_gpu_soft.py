@@ -89,16 +89,20 @@ def _dense_reference_errors(r, target):
 
 def test_soft_gradients_match_dense_torch_reference(cuda):
     """Adjoint kernel against autograd through the dense float64 PyTorch
-    restatement.  CartPole (flat cubes): tight bound.  Spheres (smooth
-    shading, near-edge-on silhouette triangles): the model itself is
-    FP32-sensitive there -- the oracle's own float32 build deviates from its
-    float64 build by up to ~5e-4 on this scene -- so the bound is looser."""
+    restatement.  The kernels compute in float32, and with the softmax
+    temperature 1e-3 the gradient is sensitive to float32 rounding of the
+    geometry: the same dense PyTorch model evaluated in float32 deviates from
+    its float64 evaluation by 6e-5 (pos), 5e-5 (scale), 2.4e-5 (hpr) on this
+    CartPole scene, and rounding only its clip coordinates to float32 already
+    costs 1.1e-5.  CartPole bound: 1.5e-4.  Spheres (smooth shading,
+    near-edge-on silhouette triangles): the oracle's own float32 build
+    deviates from its float64 build by up to ~5e-4, bound 2e-3."""
     r = soft_cartpole(4, res=48, seed=38)
     r._step(workloads.cartpole_states(4, seed=39, device=cuda))
     target = torch.rand((4, 3, 48, 48), generator=torch.Generator().manual_seed(40)).to(cuda) * 0.3
     errs = _dense_reference_errors(r, target)
     print("cartpole: gpu vs dense fp64 torch gradient relative errors:", errs)
-    assert max(errs.values()) <= 2e-5, errs
+    assert max(errs.values()) <= 1.5e-4, errs
     r = sphere_renderer()
     target = torch.rand((3, 3, 32, 40), generator=torch.Generator().manual_seed(34)).to(cuda) * 0.3
     errs = _dense_reference_errors(r, target)
@@ -154,7 +158,7 @@ def test_soft_step_and_optimisation(cuda):
         r.cart.pos.grad = None
         loss = ((soft_render(r) - target) ** 2).sum()
         loss.backward()
-        losses.append(float(loss))
+        losses.append(loss.item())
         with torch.no_grad():
             r.cart.pos[:, 0] -= 0.02 * r.cart.pos.grad[:, 0] / (r.cart.pos.grad[:, 0].abs().max() + 1e-12)
         r.cart.pos.requires_grad_(False)

@@ -43,6 +43,7 @@ struct pbr_ctx {
   // cudaFuncSetAttribute cache: [threads idx][plain][winner]
   int smem_set[3][2][2] = {};
   int small_smem_set[2][2][2] = {};
+  int soft_small_smem_set[2] = {};
   int soft_smem_set[2][2] = {};
   int soft_threads = 256;
 };
@@ -665,6 +666,61 @@ static int plan_soft(pbr_ctx* ctx, int threads, bool backward, pbr::SoftArgs* ou
   return PBR_OK;
 }
 
+// Scene-per-warp soft plan, used for both passes so that the forward and the
+// adjoint always agree on the kernel (the warp forward writes statistics only
+// where the adjoint reads them).  Sized by the adjoint's layout.
+static int plan_soft_small(pbr_ctx* ctx, bool backward, pbr::SoftArgs* out, int* smem_out, int* grid_out) {
+  const SceneParams& P = ctx->P;
+  long long tris = 0, insts = 0, verts = 0;
+  for (int n = 0; n < P.num_nodes; ++n) {
+    const NodeDesc& nd = P.nodes[n];
+    const MeshDesc& me = P.meshes[nd.mesh];
+    tris += (long long)nd.ips * me.nt;
+    insts += nd.ips;
+    verts += (long long)nd.ips * me.nv;
+  }
+  if (tris > 128 || insts > 32 || verts > 256)
+    return set_err(ctx, PBR_ERR_CAPACITY, "scene too large for the scene-per-warp soft kernel");
+  if ((P.W * P.H) % 4 != 0)  // the background is written with float4 stores per plane
+    return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp soft kernel needs W*H %% 4 == 0");
+  pbr::SoftArgs A;
+  memset(&A, 0, sizeof(A));
+  A.tri_cap = std::max(16, (int)((tris + 15) & ~15LL));
+  A.vcap = std::max(1, (int)verts);
+  A.icap = std::max(1, (int)insts);
+  A.iacc_cap = A.icap;
+  A.num_items = P.N;
+  A.status = ctx->d_status;
+  A.backward = 1;
+  const int warps = pbr::soft_small_warps();
+  const int smem_bwd = pbr::soft_small_smem_per_warp(A, P.W, P.H) * warps;
+  if (smem_bwd > ctx->max_smem)
+    return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp soft layout exceeds shared memory");
+  A.backward = backward ? 1 : 0;
+  const int smem = pbr::soft_small_smem_per_warp(A, P.W, P.H) * warps;
+  int& cached = ctx->soft_small_smem_set[backward ? 1 : 0];
+  if (smem > 48 * 1024 && smem > cached) {
+    cudaError_t e = pbr::soft_small_set_smem_limit(backward, smem);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaFuncSetAttribute");
+    cached = smem;
+  }
+  *out = A;
+  *smem_out = smem;
+  *grid_out = (P.N + warps - 1) / warps;
+  return PBR_OK;
+}
+
+// Soft kernel choice, identical for both passes: 1 = scene per warp, 2 = tile.
+static int soft_kind(pbr_ctx* ctx) {
+  if (ctx->kernel == 2) return 2;
+  pbr::SoftArgs A;
+  int smem = 0, grid = 0;
+  if (plan_soft_small(ctx, true, &A, &smem, &grid) == PBR_OK) return 1;
+  if (ctx->kernel == 1) return -1;
+  ctx->err.clear();
+  return 2;
+}
+
 int pbr_soft_config(pbr_ctx* ctx, float sigma, float gamma, int threads) {
   PBR_CHECK_CTX(ctx);
   if (!(sigma > 0.f) || !(gamma > 0.f)) return set_err(ctx, PBR_ERR_INVALID, "sigma and gamma must be positive");
@@ -694,11 +750,17 @@ int pbr_render_soft(pbr_ctx* ctx, float* d_out, float* d_stats, void* stream) {
   if (rc) return rc;
   pbr::SoftArgs A;
   int smem = 0, grid = 0;
-  rc = plan_soft(ctx, ctx->soft_threads, false, &A, &smem, &grid);
+  const int kind = soft_kind(ctx);
+  if (kind < 0) return PBR_ERR_CAPACITY;
+  if (kind == 1 && ((uintptr_t)d_out & 15u) != 0)
+    return set_err(ctx, PBR_ERR_INVALID, "d_out must be 16-byte aligned");
+  rc = kind == 1 ? plan_soft_small(ctx, false, &A, &smem, &grid)
+                 : plan_soft(ctx, ctx->soft_threads, false, &A, &smem, &grid);
   if (rc) return rc;
   A.out = d_out;
   A.stats = d_stats;
-  cudaError_t e = pbr::soft_launch(ctx->soft_threads, false, ctx->P, A, grid, smem, (cudaStream_t)stream);
+  cudaError_t e = kind == 1 ? pbr::soft_small_launch(false, ctx->P, A, grid, smem, (cudaStream_t)stream)
+                            : pbr::soft_launch(ctx->soft_threads, false, ctx->P, A, grid, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_err(ctx, e, "soft forward launch");
   return PBR_OK;
 }
@@ -715,14 +777,17 @@ int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, co
       return set_err(ctx, PBR_ERR_STATE, "soft backward needs every node in HPR mode (node %d is not)", n);
   pbr::SoftArgs A;
   int smem = 0, grid = 0;
-  // the adjoint keeps 15 values per pixel in shared memory: 128-thread CTAs
-  rc = plan_soft(ctx, 128, true, &A, &smem, &grid);
+  const int kind = soft_kind(ctx);
+  if (kind < 0) return PBR_ERR_CAPACITY;
+  // the tile adjoint keeps 15 values per pixel in shared memory: 128-thread CTAs
+  rc = kind == 1 ? plan_soft_small(ctx, true, &A, &smem, &grid) : plan_soft(ctx, 128, true, &A, &smem, &grid);
   if (rc) return rc;
   A.out = const_cast<float*>(d_out);
   A.stats = const_cast<float*>(d_stats);
   A.gout = d_grad_out;
   A.glight = d_grad_light;
-  cudaError_t e = pbr::soft_launch(128, true, ctx->P, A, grid, smem, (cudaStream_t)stream);
+  cudaError_t e = kind == 1 ? pbr::soft_small_launch(true, ctx->P, A, grid, smem, (cudaStream_t)stream)
+                            : pbr::soft_launch(128, true, ctx->P, A, grid, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_err(ctx, e, "soft backward launch");
   return PBR_OK;
 }

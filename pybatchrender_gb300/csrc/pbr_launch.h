@@ -26,6 +26,12 @@ int soft_smem_bytes(const SoftArgs& a, int threads);
 cudaError_t soft_set_smem_limit(int threads, bool backward, int bytes);
 cudaError_t soft_launch(int threads, bool backward, const SceneParams& P, const SoftArgs& A, int grid, int smem_bytes,
                         cudaStream_t stream);
+// Scene-per-warp soft coverage (pbr_soft_small.cu); blocks of soft_small_warps() warps.
+int soft_small_warps();
+int soft_small_smem_per_warp(const SoftArgs& a, int W, int H);
+cudaError_t soft_small_set_smem_limit(bool backward, int bytes);
+cudaError_t soft_small_launch(bool backward, const SceneParams& P, const SoftArgs& A, int grid, int smem_bytes,
+                              cudaStream_t stream);
 cudaError_t plain_clear_launch(const SceneParams& P, float* zbuf, uint32_t* cbuf, cudaStream_t stream);
 cudaError_t plain_resolve_launch(const SceneParams& P, const float* zbuf, const uint32_t* cbuf, uint8_t* out,
                                  float* depth, cudaStream_t stream);

@@ -3,21 +3,25 @@
 Workload (headline): CartPole render, 4096 scenes x 64x64 RGB uint8, two unit
 cubes per scene (the benchmark CartPole scene of pybatchrender_gb300.workloads),
 seeded synthetic states.  A step = write the step's states into the scene
-(``_step``) + one render of all scenes.  One frame = one scene image
-(steps x scenes / s, as the reference's cartpole benchmark counts).
++ one render of all scenes: ``step(state)``, which for this scene is one
+kernel launch (the cart x, pole x and pole pitch columns of the state are
+bound to the node poses with ``bind_state`` and read by the raster launch).
+One frame = one scene image (steps x scenes / s, as the reference's cartpole
+benchmark counts).
 
 Reported variants (all on the same scene and states):
-  value        batched renderer, whole step captured in a CUDA graph, inputs
-               resident in HBM; per-step CUDA-event time with the L2 flushed
-               (a 256 MiB write) before every step, flush excluded.
+  value        the step above, inputs resident in HBM; per-step CUDA-event
+               time with the L2 flushed (a 256 MiB write) before every step,
+               flush excluded.
   e2e          the same call through the public API with host buffers:
                states copied from pinned host memory and pixels copied back to
                pinned host memory inside the timed region (wall clock).
   variants     plain per-launch path (host-built matrices, a host-to-device
-               copy per node, one launch per node, a synchronise), batched
-               eager (no graph), batched graph; soft_fwd (differentiable
-               soft-coverage forward, float32) and fwd_bwd (soft forward +
-               adjoint kernel with a constant dL/dout) on the same scene.
+               copy per node, one launch per node, a synchronise); the step
+               through ``_step``'s torch copies + render captured in a CUDA
+               graph; soft_fwd (differentiable soft-coverage forward, float32)
+               and fwd_bwd (soft forward + adjoint kernel with a constant
+               dL/dout) on the same scene.
   roofline     the hard-raster kernel alone: algorithmic bytes per launch /
                mean CUDA-event duration, against the measured HBM copy peak.
   cpu_baseline the oracle's FP32 rasteriser (a CPU port of the reference's
@@ -247,16 +251,24 @@ def run_ours(args, world, rank, local):
         eager_r.cfg.persistent, eager_r.cfg.tri_cap = bool(tuned["persistent"]), tuned["tri_cap"]
         eager_r._build_context()
     plain_r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", raster_method="plain")
+    # the same step through _step's torch copies, graph-captured (no state binding)
+    copy_r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", cuda_graph=True)
+    copy_r._state_bindings = []
+    if tuned:
+        copy_r.cfg.raster_kernel = tuned["kernel"]
+        copy_r.cfg.raster_threads, copy_r.cfg.bin_size = tuned["threads"], tuned["bin_px"]
+        copy_r.cfg.persistent, copy_r.cfg.tri_cap = bool(tuned["persistent"]), tuned["tri_cap"]
+        copy_r._build_context()
     states_cpu = [s.cpu() for s in states]
 
     with ClockSampler(local) as clocks:
         # warm-up (graph capture happens on the first step)
         for i in range(max(3, args.warmup)):
             graph_r.step(states[i % 16])
-            eager_r.step(states[i % 16])
+            copy_r.step(states[i % 16])
         torch.cuda.synchronize()
 
-        # headline: graph-captured batched step, inputs resident in HBM
+        # headline: the env step (state -> poses -> pixels) as one launch, inputs resident in HBM
         barrier(world)
         t = time_steps(lambda i: graph_r.step(states[i % 16]), args.steps, flush, stream)
         barrier(world)
@@ -264,9 +276,9 @@ def run_ours(args, world, rank, local):
         ms_per_step = graph_ms / args.steps
         value = world * N * args.steps / (graph_ms / 1000.0)
 
-        # batched, no graph
-        t = time_steps(lambda i: eager_r.step(states[i % 16]), args.steps, flush, stream)
-        eager_fps = N * args.steps / (reduce_max(sum(t), world) / 1000.0)
+        # the same step with _step's torch copies, captured in a CUDA graph with the render
+        t = time_steps(lambda i: copy_r.step(states[i % 16]), args.steps, flush, stream)
+        copy_fps = N * args.steps / (reduce_max(sum(t), world) / 1000.0)
 
         # plain per-launch path (wall clock: it synchronises every step)
         plain_steps = max(3, min(args.steps, args.plain_steps))
@@ -335,11 +347,13 @@ def run_ours(args, world, rank, local):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": f"cartpole_bench {N} scenes {res}x{res} RGB u8, 2 unit cubes/scene, seeded states",
+                   "step": "state [N,4] -> cart x, pole x, pole pitch -> pixels in one launch (state columns bound "
+                           "to poses); variants.batched_graph_step_copies = _step torch copies + render in a graph",
                    "global_batch": N * world, "parallelism": f"replicas x{world}",
                    "l2": "flushed (256 MiB write) before every timed step, flush excluded",
                    "launch": tuned or {"kernel": graph_r.cfg.raster_kernel, "threads": graph_r.cfg.raster_threads,
                                        "bin_px": graph_r.cfg.bin_size}},
-        "variants": {"batched_graph": value / world, "batched_eager": eager_fps, "plain": plain_fps,
+        "variants": {"batched_fused_step": value / world, "batched_graph_step_copies": copy_fps, "plain": plain_fps,
                      "graph_over_plain": (value / world) / plain_fps,
                      "soft_fwd": soft_fwd_fps, "fwd_bwd": fwd_bwd_fps, "soft_fwd_over_fwd_bwd": soft_fwd_fps / fwd_bwd_fps},
         "e2e": {"value": e2e_fps, "unit": UNIT, "h2d_bytes_per_step": int(N * 4 * 4),

@@ -90,6 +90,22 @@ int pbr_node_add(pbr_ctx* ctx, int mesh_id, int instances_per_scene, int shared,
 int pbr_node_set_buffers(pbr_ctx* ctx, int node_id, int mode, const float* d_pos, const float* d_rot,
                          const float* d_scale, const float* d_color, const int32_t* d_counts);
 
+/* Bind pose component `component` of a node to column `column` of a per-step
+ * state matrix: 0..2 = position x, y, z; 3..5 = heading, pitch, roll (HPR
+ * mode).  column < 0 removes the binding.  Buffer row r of the node reads
+ * state row r (scene k, instance i of a per-scene node: row
+ * k*instances_per_scene + i).  The bound values are used by
+ * pbr_render_state only.  Replaces an env's _step() that copies state
+ * columns into node poses (envs/cartpole/renderer.py:98-140 copies cart x,
+ * pole x and pole pitch): the copy happens inside the raster launch. */
+int pbr_node_bind_state(pbr_ctx* ctx, int node_id, int component, int column);
+
+/* Set (d_state non-NULL) or clear (NULL) the state matrix the bound pose
+ * components read: float32, `rows` rows of `cols` values, row r at
+ * d_state + r*row_stride.  Checked against every binding (column < cols,
+ * enough rows, angles only on HPR-mode nodes). */
+int pbr_state_source(pbr_ctx* ctx, const float* d_state, long long rows, int cols, long long row_stride);
+
 /* Bind the per-scene view-projection matrices d_vp [N,16] (row-major, GL
  * clip-space conventions) and the camera's near/far planes (used by the soft
  * mode's depth normalisation).  Replaces viewbuf (renderer/camera.py:146-148,
@@ -132,6 +148,15 @@ int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_kernel, in
  * Replaces taskMgr.step() + grab_pixels +
  * _rearrange_img (renderer/renderer.py:377-390,326-363). */
 int pbr_render(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, int32_t* d_winner, void* stream);
+
+/* pbr_render with the state-bound pose components read from d_state (see
+ * pbr_node_bind_state) and written back into the node's pose buffers, as
+ * an explicit per-step copy would leave them: one launch for the whole
+ * env step.  The source is cleared again before returning.  No reference
+ * counterpart (the reference copies state into poses on the host, then
+ * draws). */
+int pbr_render_state(pbr_ctx* ctx, const float* d_state, long long rows, int cols, long long row_stride,
+                     uint8_t* d_out, float* d_depth, int32_t* d_winner, void* stream);
 
 /* "Plain" per-node path that mirrors the reference's per-step flow (one draw
  * per node into a depth/colour buffer, then a readback into [N,C,H,W]):

@@ -42,6 +42,9 @@ SIGNATURES: dict[str, list] = {
     "pbr_raster_config": [_vp, _i, _i, _i, _i, _i],
     "pbr_autotune": [_vp, _vp, _vp, _pi, _pi, _pi, _pi, _pi, _pf],
     "pbr_render": [_vp, _vp, _vp, _vp, _vp],
+    "pbr_node_bind_state": [_vp, _i, _i, _i],
+    "pbr_state_source": [_vp, _vp, ctypes.c_longlong, _i, ctypes.c_longlong],
+    "pbr_render_state": [_vp, _vp, ctypes.c_longlong, _i, ctypes.c_longlong, _vp, _vp, _vp, _vp],
     "pbr_plain_clear": [_vp, _vp],
     "pbr_plain_draw": [_vp, _i, _vp],
     "pbr_plain_resolve": [_vp, _vp, _vp, _vp],

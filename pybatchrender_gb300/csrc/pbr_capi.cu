@@ -374,6 +374,7 @@ int pbr_node_add(pbr_ctx* ctx, int mesh_id, int instances_per_scene, int shared,
   nd.ips = instances_per_scene;
   nd.shared = shared ? 1 : 0;
   nd.mode = pbr::kModeHpr;
+  for (int c = 0; c < 8; ++c) nd.src_col[c] = -1;
   int rank = 0;
   for (int i = 0; i < n; ++i) rank += ctx->P.nodes[i].ips;
   nd.rank_base = rank;
@@ -401,6 +402,46 @@ int pbr_node_set_buffers(pbr_ctx* ctx, int node_id, int mode, const float* d_pos
   nd.color = d_color;
   nd.counts = d_counts;
   ctx->node_ready[node_id] = true;
+  return PBR_OK;
+}
+
+int pbr_node_bind_state(pbr_ctx* ctx, int node_id, int component, int column) {
+  PBR_CHECK_CTX(ctx);
+  if (node_id < 0 || node_id >= ctx->P.num_nodes) return set_err(ctx, PBR_ERR_INVALID, "unknown node id %d", node_id);
+  if (component < 0 || component > 5)
+    return set_err(ctx, PBR_ERR_INVALID, "component must be 0..2 (position) or 3..5 (heading, pitch, roll)");
+  if (column > 127) return set_err(ctx, PBR_ERR_INVALID, "state column must be < 128");
+  ctx->P.nodes[node_id].src_col[component] = (int8_t)(column < 0 ? -1 : column);
+  return PBR_OK;
+}
+
+int pbr_state_source(pbr_ctx* ctx, const float* d_state, long long rows, int cols, long long row_stride) {
+  PBR_CHECK_CTX(ctx);
+  SceneParams& P = ctx->P;
+  if (d_state) {
+    if (rows < 0 || cols < 0 || row_stride < cols)
+      return set_err(ctx, PBR_ERR_INVALID, "state matrix needs rows >= 0 and row_stride >= cols >= 0");
+    for (int n = 0; n < P.num_nodes; ++n) {
+      const NodeDesc& nd = P.nodes[n];
+      const long long need = nd.shared ? (long long)nd.ips : (long long)nd.ips * P.N;
+      for (int c = 0; c < 6; ++c) {
+        if (nd.src_col[c] < 0) continue;
+        if (nd.src_col[c] >= cols)
+          return set_err(ctx, PBR_ERR_INVALID, "node %d binds column %d of a %d-column state", n, nd.src_col[c], cols);
+        if (need > rows)
+          return set_err(ctx, PBR_ERR_INVALID, "node %d needs %lld state rows, got %lld", n, need, rows);
+        if (c >= 3 && nd.mode != pbr::kModeHpr)
+          return set_err(ctx, PBR_ERR_STATE, "node %d binds an angle but is not in HPR mode", n);
+      }
+    }
+  }
+  for (int n = 0; n < P.num_nodes; ++n) {
+    NodeDesc& nd = P.nodes[n];
+    bool any = false;
+    for (int c = 0; c < 6; ++c) any = any || nd.src_col[c] >= 0;
+    nd.src = (d_state && any) ? d_state : nullptr;
+    nd.src_stride = row_stride;
+  }
   return PBR_OK;
 }
 
@@ -484,6 +525,17 @@ int pbr_render(pbr_ctx* ctx, uint8_t* d_out, float* d_depth, int32_t* d_winner, 
   int rc = check_ready(ctx, 0, ctx->P.num_nodes);
   if (rc) return rc;
   return render_with(ctx, ctx_cfg(ctx), d_out, d_depth, d_winner, (cudaStream_t)stream);
+}
+
+int pbr_render_state(pbr_ctx* ctx, const float* d_state, long long rows, int cols, long long row_stride,
+                     uint8_t* d_out, float* d_depth, int32_t* d_winner, void* stream) {
+  PBR_CHECK_CTX(ctx);
+  if (!d_state) return set_err(ctx, PBR_ERR_INVALID, "d_state is null");
+  int rc = pbr_state_source(ctx, d_state, rows, cols, row_stride);
+  if (rc) return rc;
+  rc = pbr_render(ctx, d_out, d_depth, d_winner, stream);
+  pbr_state_source(ctx, nullptr, 0, 0, 0);  // the launch has its copy of the parameters
+  return rc;
 }
 
 int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_kernel, int* out_threads, int* out_bin_px,

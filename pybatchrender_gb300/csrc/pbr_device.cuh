@@ -44,6 +44,13 @@ __device__ __forceinline__ void shade_rgb(const SceneParams& P, float nx, float 
   out[2] = col.z * ((1.f - s) + (P.amb[2] + ndl * P.lcol[2]) * s);
 }
 
+// Pose component c (0..2 position, 3..5 HPR) of buffer row `id`: from the
+// bound state matrix when the node has one for c, else from *own.
+__device__ __forceinline__ float bound_value(const NodeDesc& nd, long long id, int c, const float* own) {
+  if (nd.src && nd.src_col[c] >= 0) return nd.src[id * nd.src_stride + nd.src_col[c]];
+  return *own;
+}
+
 // Model matrix rows (3x4, row-major) of buffer row `id` of a node.
 __device__ __forceinline__ void build_model(const NodeDesc& nd, long long id, float m[12]) {
   if (nd.mode == kModeMat) {
@@ -54,7 +61,9 @@ __device__ __forceinline__ void build_model(const NodeDesc& nd, long long id, fl
   }
   float R[9];
   if (nd.mode == kModeHpr) {
-    const float* a = nd.rot + id * 3;
+    float a[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) a[c] = bound_value(nd, id, 3 + c, nd.rot + id * 3 + c);
     float sh, ch, sp, cp, sr, cr;
     sincosf(a[0], &sh, &ch);
     sincosf(a[1], &sp, &cp);
@@ -69,13 +78,25 @@ __device__ __forceinline__ void build_model(const NodeDesc& nd, long long id, fl
     for (int i = 0; i < 9; ++i) R[i] = a[i];
   }
   const float s = nd.scale[id];
-  const float* p = nd.pos + id * 3;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     m[r * 4 + 0] = R[r * 3 + 0] * s;
     m[r * 4 + 1] = R[r * 3 + 1] * s;
     m[r * 4 + 2] = R[r * 3 + 2] * s;
-    m[r * 4 + 3] = p[r];
+    m[r * 4 + 3] = bound_value(nd, id, r, nd.pos + id * 3 + r);
+  }
+}
+
+// Copy the state-bound pose components of buffer row `id` into the node's own
+// pose buffers, so that they hold what an explicit per-step copy would.
+__device__ __forceinline__ void write_back_bound(const NodeDesc& nd, long long id) {
+  if (!nd.src) return;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    if (nd.src_col[c] >= 0) {
+      float* dst = const_cast<float*>(c < 3 ? nd.pos + id * 3 + c : nd.rot + id * 3 + (c - 3));
+      *dst = nd.src[id * nd.src_stride + nd.src_col[c]];
+    }
   }
 }
 

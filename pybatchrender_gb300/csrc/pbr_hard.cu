@@ -348,6 +348,7 @@ __global__ void __launch_bounds__(THREADS) hard_kernel(const __grid_constant__ S
           const long long id = nd.shared ? (long long)(b0 + i) : (long long)k * nd.ips + b0 + i;
           float m[12];
           build_model(nd, id, m);
+          if (r == 0) write_back_bound(nd, id);
           icache[i * 4 + 0] = make_float4(m[0], m[1], m[2], m[3]);
           icache[i * 4 + 1] = make_float4(m[4], m[5], m[6], m[7]);
           icache[i * 4 + 2] = make_float4(m[8], m[9], m[10], m[11]);

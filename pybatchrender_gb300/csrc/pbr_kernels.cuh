@@ -43,6 +43,11 @@ struct NodeDesc {
   float* gcol;
   int32_t mesh, ips, shared, mode;
   int32_t rank_base, pad0, pad1, pad2;
+  // state binding: position component c (0..2) / HPR angle c (3..5) of buffer
+  // row r is src[r * src_stride + src_col[c]] when src is set and src_col[c] >= 0
+  const float* src;
+  int64_t src_stride;
+  int8_t src_col[8];
 };
 
 struct SceneParams {

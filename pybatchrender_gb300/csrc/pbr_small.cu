@@ -221,6 +221,7 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
       const long long id = nd.shared ? (long long)li : (long long)k * nd.ips + li;
       float m[12];
       build_model(nd, id, m);
+      write_back_bound(nd, id);
       float4* e = itab + i * 5;
       e[0] = make_float4(m[0], m[1], m[2], m[3]);
       e[1] = make_float4(m[4], m[5], m[6], m[7]);

@@ -54,6 +54,10 @@ class CartPoleRenderer(PBRRenderer):
         self._pbr_cam.set_positions(torch.tensor([5, 5, 2], dtype=torch.float32))
         self._pbr_cam.look_at(torch.tensor([0, 0, 0], dtype=torch.float32))
         self.add_light()
+        # the copies of _step, done inside the raster launch when step() gets a CUDA state
+        self.bind_state(self.cart, "x", 0)
+        self.bind_state(self.pole, "x", 0)
+        self.bind_state(self.pole, "p", 2)
         self.setup_environment()
 
     def _step(self, state_batch: torch.Tensor | None = None):

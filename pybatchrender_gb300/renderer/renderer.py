@@ -63,6 +63,7 @@ class PBRRenderer:
         self._static_depth = None
         self._plain_staging: dict = {}
         self.autotune_result = None
+        self._state_bindings: list[tuple[PBRNode, int, int]] = []
 
     # ------------------------------------------------------------- scene API
     def set_background_color(self, r: float, g: float, b: float, a: float = 1.0) -> None:
@@ -130,6 +131,66 @@ class PBRRenderer:
         if self.cfg.autotune and self.cfg.raster_method == "batched" and self.cfg.raster_mode == "hard":
             self.autotune()
 
+    # ----------------------------------------------------------- state binding
+    POSE_COMPONENTS = {"x": 0, "y": 1, "z": 2, "h": 3, "p": 4, "r": 5}
+
+    def bind_state(self, node: PBRNode, component, column: int) -> None:
+        """Declare that pose ``component`` of ``node`` (``"x"``, ``"y"``,
+        ``"z"`` position or ``"h"``, ``"p"``, ``"r"`` HPR angle in radians;
+        or 0..5) equals column ``column`` of the state passed to ``step``.
+
+        When every argument of ``step`` is a single CUDA float32 ``[N, S]``
+        state (one row per scene; row ``k * instances_per_scene + i`` for
+        nodes with several instances), the bound components are read by the
+        raster launch itself and written back into the node's tensors, and
+        ``_step`` is not called: the env step is one kernel launch.  Any other
+        argument falls back to ``_step`` + render, so ``_step`` must still
+        perform the same copies."""
+        comp = self.POSE_COMPONENTS[component] if isinstance(component, str) else int(component)
+        if not 0 <= comp <= 5:
+            raise ValueError("component must be x, y, z, h, p, r or 0..5")
+        if column < 0:
+            raise ValueError("column must be >= 0")
+        if comp >= 3 and node.mode != _capi.MODE_HPR:
+            raise ValueError("angle bindings need a node in HPR mode")
+        self._state_bindings = [b for b in self._state_bindings if not (b[0] is node and b[1] == comp)]
+        self._state_bindings.append((node, comp, int(column)))
+        self._graph = None
+        if self._ctx is not None and node in self._node_ids:
+            _capi.call(self._lib, self._ctx, "pbr_node_bind_state", self._node_ids[node], comp, int(column))
+
+    def _bound_state(self, args, kwargs):
+        """The state tensor of a step that can take the fused path, else None."""
+        if not self._state_bindings or kwargs or len(args) != 1 or self._ctx is None:
+            return None
+        s = args[0]
+        if not (torch.is_tensor(s) and s.device == self.device and s.dtype == torch.float32 and s.dim() == 2
+                and s.stride(1) == 1 and s.shape[0] == self.num_scenes and not s.requires_grad):
+            return None
+        if max(col for _, _, col in self._state_bindings) >= s.shape[1]:
+            return None
+        for node, comp, _ in self._state_bindings:
+            if node.shared_across or node.instances_per_scene != 1 or node.mode == _capi.MODE_MAT \
+                    or (comp >= 3 and node.mode != _capi.MODE_HPR):
+                return None
+        return s
+
+    def _render_state(self, state: torch.Tensor):
+        N, C, H, W = self._out_shape()
+        want_depth = self.cfg.return_depth
+        if self.cfg.reuse_output or self.cfg.cuda_graph:
+            if self._static_out is None:
+                self._static_out = torch.empty((N, C, H, W), dtype=torch.uint8, device=self.device)
+            if want_depth and self._static_depth is None:
+                self._static_depth = torch.empty((N, H, W), dtype=torch.float32, device=self.device)
+            out, depth = self._static_out, (self._static_depth if want_depth else None)
+        else:
+            out = torch.empty((N, C, H, W), dtype=torch.uint8, device=self.device)
+            depth = torch.empty((N, H, W), dtype=torch.float32, device=self.device) if want_depth else None
+        _capi.call(self._lib, self._ctx, "pbr_render_state", _capi.ptr(state), int(state.shape[0]),
+                   int(state.shape[1]), int(state.stride(0)), _capi.ptr(out), _capi.ptr(depth), None, self._stream())
+        return (out, depth) if want_depth else out
+
     # ---------------------------------------------------------------- stepping
     def _step(self, *args, **kwargs):
         """Subclass hook: write the scene state for this step (default no-op)."""
@@ -143,8 +204,13 @@ class PBRRenderer:
         ``[N,C,H,W]`` on the CUDA device (plus float32 ``[N,H,W]`` depth when
         ``cfg.return_depth``), ``None`` when ``return_pixels`` is False
         (``renderer.py:377-390``)."""
-        if self.cfg.cuda_graph and return_pixels and not self.cfg.interactive \
-                and self.cfg.raster_method == "batched" and self.cfg.raster_mode == "hard":
+        fused = return_pixels and not self.cfg.interactive and self.cfg.raster_method == "batched" \
+            and self.cfg.raster_mode == "hard"
+        if fused:
+            state = self._bound_state(args, kwargs)
+            if state is not None:
+                return self._render_state(state)
+        if self.cfg.cuda_graph and fused:
             return self._graph_step(args, kwargs)
         if not getattr(self.cfg, "interactive", False):
             self._step(*args, **kwargs)
@@ -418,6 +484,9 @@ class PBRRenderer:
                            int(node.shared_across), ctypes.byref(nid))
                 self._node_ids[node] = nid.value
                 self._bind_node_buffers(node)
+            for node, comp, col in self._state_bindings:
+                if node in self._node_ids:
+                    _capi.call(lib, ctx, "pbr_node_bind_state", self._node_ids[node], comp, col)
             self._camera_changed(self._pbr_cam)
             self._light_changed(self._pbr_light)
             _capi.call(lib, ctx, "pbr_background_set", (ctypes.c_float * 4)(*self._background_color))

@@ -54,6 +54,10 @@ class CartPoleBenchRenderer(PBRRenderer):
         self.add_camera(fov_y_deg=40.0)
         self._pbr_cam.set_positions_and_lookat(torch.tensor([0.0, -8.0, 1.5]), torch.tensor([0.0, 0.0, 0.0]))
         self.add_light(ambient=(0.2, 0.2, 0.2), dir_dir=(0.3, -1.0, -0.5))
+        # the copies of _step, done inside the raster launch when step() gets a CUDA state
+        self.bind_state(self.cart, "x", 0)
+        self.bind_state(self.pole, "x", 0)
+        self.bind_state(self.pole, "p", 2)
         self.setup_environment()
 
     def _step(self, state: torch.Tensor | None = None):

@@ -133,3 +133,20 @@ def test_atlas_roundtrip():
     atlas = r.to_atlas(pix)
     assert atlas.shape == (2 * 6, 3 * 8, 3)
     assert torch.equal(r._rearrange_img(atlas), pix)
+
+
+def test_bind_state_validation():
+    r = workloads.cartpole_bench(num_scenes=4, res=32, device="cpu")
+    assert {(b[1], b[2]) for b in r._state_bindings} == {(0, 0), (4, 2)}
+    r.bind_state(r.cart, "y", 1)
+    assert (r.cart, 1, 1) in r._state_bindings
+    r.bind_state(r.cart, "y", 3)  # rebinding replaces
+    assert (r.cart, 1, 1) not in r._state_bindings and (r.cart, 1, 3) in r._state_bindings
+    with pytest.raises(KeyError):
+        r.bind_state(r.cart, "w", 0)
+    with pytest.raises(ValueError):
+        r.bind_state(r.cart, 6, 0)
+    with pytest.raises(ValueError):
+        r.bind_state(r.cart, "x", -1)
+    # no CUDA context: the fused path is never taken
+    assert r._bound_state((torch.zeros(4, 4),), {}) is None

@@ -372,6 +372,105 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_workload(args, world, rank, local):
+    """One of the other configurations, on its own JSON line (not the headline):
+    many_cubes (1024 scenes 128x128 RGB + depth, 64 cubes), uneven (4096 scenes
+    84x84, 1..512 instances of mixed meshes, graph-captured step with in-place
+    pose updates), soft_cartpole (512 scenes 64x64 soft forward + adjoint),
+    soft_large (16384 scenes 128x128 soft forward + adjoint, 128 instances)."""
+    from pybatchrender_gb300 import _capi, workloads
+
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    _capi.load(build_if_missing=True)
+    stream = torch.cuda.current_stream(device)
+    flush = l2_flusher(device)
+    name = args.workload
+    hbm_peak, peak_src = measured_peak()
+    line = {"workload": name, "unit": UNIT, "n_gpus": world, "higher_is_better": True, "scaling": "weak",
+            "data": "synthetic", "steps": args.steps, "warmup": args.warmup}
+    torch.cuda.reset_peak_memory_stats(device)
+    if name in ("many_cubes", "uneven"):
+        ns = {"num_scenes": args.workload_scenes} if args.workload_scenes > 0 else {}
+        if name == "many_cubes":
+            r = workloads.many_cubes(seed=rank, return_depth=True, reuse_output=True, **ns)
+            n_inst = 64.0
+            px_bytes = 3 + 4
+            desc = f"{r.num_scenes} scenes 128x128 RGB u8 + f32 depth, 64 unit cubes/scene, random poses, hard raster"
+        else:
+            r = workloads.uneven(seed=rank, cuda_graph=True, persistent=True, **ns)
+            n_inst = float(r.total_counts.float().mean())
+            px_bytes = 3
+            desc = (f"{r.num_scenes} scenes 84x84 RGB u8, log-uniform 1..512 instances/scene of cube/cylinder-64/icosphere-3, "
+                    "per-scene camera, step = in-place HPR update + render, CUDA graph, persistent launch")
+            nodes = r.uneven_nodes
+
+            def upd():
+                for nd in nodes:
+                    nd.hpr.add_(0.01)
+            r._step = lambda *a, **k: upd()
+        tuned = r.autotune() if args.autotune else None
+        N = r.num_scenes
+        W, H = r.cfg.tile_resolution
+        step = (lambda i: r.step()) if name == "uneven" else (lambda i: r.render())
+        for i in range(max(3, args.warmup)):
+            step(i)
+        torch.cuda.synchronize()
+        t = time_steps(step, args.steps, flush, stream)
+        ms = reduce_max(sum(t), world) / args.steps
+        bpf = W * H * px_bytes + n_inst * BYTES_PER_INSTANCE + BYTES_PER_SCENE
+        fps = world * N / (ms / 1000.0)
+        line.update({"metric": f"frames/s, {name}", "value": fps, "ms_per_step": ms, "dtype": "u8",
+                     "config": {"workload": desc, "launch": tuned, "mean_instances": n_inst},
+                     "roofline": {"bound": "hbm", "achieved": bpf * N / (ms / 1000.0) / 1e9, "peak": hbm_peak,
+                                  "unit": "GB/s", "frac": bpf * N / (ms / 1000.0) / 1e9 / hbm_peak,
+                                  "bytes_per_frame": bpf, "peak_source": peak_src}})
+    else:
+        if name == "soft_cartpole":
+            N, res = args.workload_scenes or 512, 64
+            r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", raster_mode="soft")
+            n_inst = 2
+            desc = f"{N} scenes 64x64 f32 soft coverage (sigma 0.5 px edge, gamma 1e-3), CartPole bench scene"
+            states = [workloads.cartpole_states(N, seed=100 + i, device=device) for i in range(16)]
+            pre = lambda i: r._step(states[i % 16])
+        else:
+            N, res = args.workload_scenes or 16384, 128
+            r = workloads.soft_large(num_scenes=N, res=res, seed=rank)
+            n_inst = 128
+            desc = f"{N} scenes 128x128 f32 soft coverage, 128 instances/scene (64 icosphere-s2 + 64 cubes)"
+            pre = lambda i: None
+        gout = torch.full((N, 3, res, res), 1.0 / (N * 3 * res * res), device=device)
+
+        def fwd(i):
+            pre(i)
+            r._soft_forward(None)
+
+        def fwd_bwd(i):
+            pre(i)
+            out, st = r._soft_forward(None)
+            r._soft_backward(out, st, gout)
+        for i in range(max(3, args.warmup)):
+            fwd_bwd(i)
+        torch.cuda.synchronize()
+        tf = time_steps(fwd, args.steps, flush, stream)
+        tb = time_steps(fwd_bwd, args.steps, flush, stream)
+        ms_f = reduce_max(sum(tf), world) / args.steps
+        ms_b = reduce_max(sum(tb), world) / args.steps
+        b_fwd = res * res * 12 + n_inst * BYTES_PER_INSTANCE + BYTES_PER_SCENE
+        b_bwd = b_fwd + res * res * 12 + n_inst * 36 + 12
+        line.update({"metric": f"frames/s, {name} forward + adjoint", "value": world * N / (ms_b / 1000.0),
+                     "ms_per_step": ms_b, "dtype": "f32",
+                     "forward": {"value": world * N / (ms_f / 1000.0), "ms_per_step": ms_f},
+                     "fwd_over_fwd_bwd": ms_b / ms_f,
+                     "config": {"workload": desc},
+                     "roofline": {"bound": "hbm", "achieved": b_bwd * N / (ms_b / 1000.0) / 1e9, "peak": hbm_peak,
+                                  "unit": "GB/s", "frac": b_bwd * N / (ms_b / 1000.0) / 1e9 / hbm_peak,
+                                  "bytes_per_frame": b_bwd, "peak_source": peak_src}})
+    line["hbm_footprint_bytes"] = int(torch.cuda.max_memory_allocated(device))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -385,11 +484,18 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--cpu-budget", type=float, default=10.0)
+    ap.add_argument("--workload-scenes", type=int, default=0,
+                    help="scene count for --workload (0: the configuration's own; smaller for profiling)")
+    ap.add_argument("--workload", default="cartpole",
+                    choices=["cartpole", "many_cubes", "uneven", "soft_cartpole", "soft_large"],
+                    help="cartpole = the headline; the others print their own line (see run_workload)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     try:
         if args.impl == "reference":
             run_reference(args, world, rank)
+        elif args.workload != "cartpole":
+            run_workload(args, world, rank, local)
         else:
             run_ours(args, world, rank, local)
     finally:

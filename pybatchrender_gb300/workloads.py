@@ -148,3 +148,26 @@ def uneven(num_scenes: int = 4096, res: int = 84, max_instances: int = 512, seed
     r.add_light()
     r.setup_environment()
     return r
+
+
+def soft_large(num_scenes: int = 16384, res: int = 128, instances: int = 128, seed: int = 0, **cfg) -> PBRRenderer:
+    """Large soft-coverage workload: per scene ``instances`` non-shared
+    instances, half icosphere-s2 (320 triangles, smooth) and half unit cubes
+    (12 triangles, flat), random poses as in :func:`many_cubes`."""
+    r = PBRRenderer(PBRConfig(num_scenes=num_scenes, tile_resolution=(res, res), report_fps=False,
+                              raster_mode="soft", **cfg))
+    g = _gen(seed)
+    r.soft_nodes = []
+    for m in ("icosphere:2", "models/box"):
+        node = r.add_node(m, instances // 2, model_pivot_relative_point=(0.5, 0.5, 0.5))
+        pos, hpr, scale, col = _random_poses(node.buf_instances, g)
+        node.set_positions(pos)
+        node.set_hprs(hpr)
+        node.set_scales(scale)
+        node.set_colors(col)
+        r.soft_nodes.append(node)
+    r.add_camera(fov_y_deg=45.0)
+    r._pbr_cam.set_positions_and_lookat(torch.tensor([0.0, -12.0, 0.0]), torch.tensor([0.0, 0.0, 0.0]))
+    r.add_light()
+    r.setup_environment()
+    return r

@@ -749,6 +749,9 @@ static int plan_soft_small(pbr_ctx* ctx, bool backward, pbr::SoftArgs* out, int*
   if (smem_bwd > ctx->max_smem)
     return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp soft layout exceeds shared memory");
   A.backward = backward ? 1 : 0;
+  // few scenes: several warps per scene (each takes every split-th pixel block) so that ~16 warps per SM work
+  const long long want = (long long)ctx->sm_count * 16;
+  A.split = (int)std::min<long long>(4, std::max<long long>(1, (want + P.N - 1) / std::max(1, P.N)));
   const int smem = pbr::soft_small_smem_per_warp(A, P.W, P.H) * warps;
   int& cached = ctx->soft_small_smem_set[backward ? 1 : 0];
   if (smem > 48 * 1024 && smem > cached) {
@@ -758,7 +761,7 @@ static int plan_soft_small(pbr_ctx* ctx, bool backward, pbr::SoftArgs* out, int*
   }
   *out = A;
   *smem_out = smem;
-  *grid_out = (P.N + warps - 1) / warps;
+  *grid_out = (int)(((long long)P.N * A.split + warps - 1) / warps);
   return PBR_OK;
 }
 

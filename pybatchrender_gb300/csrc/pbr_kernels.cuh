@@ -95,6 +95,7 @@ struct SoftArgs {
   int32_t region_px, regions_per_scene, num_items;
   int32_t bin_px, bins_x, max_region_bins;
   int32_t backward;
+  int32_t split;  // scene-per-warp soft kernel: warps per scene (each takes every split-th pixel block)
 };
 
 struct SoftLayout {

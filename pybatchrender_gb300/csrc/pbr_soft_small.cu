@@ -96,7 +96,10 @@ __global__ void __launch_bounds__(kSoftWarps * 32) soft_small_kernel(const __gri
   const float inv_gamma = 1.f / P.gamma;
   const int lx = lane & (kBlkW - 1), ly = lane / kBlkW;
 
-  for (int k = blockIdx.x * kSoftWarps + warp; k < P.N; k += gridDim.x * kSoftWarps) {
+  const int split = max(1, A.split);
+  for (int gw = blockIdx.x * kSoftWarps + warp; gw / split < P.N; gw += gridDim.x * kSoftWarps) {
+    // scene k; this warp takes the pixel blocks b with b % split == sub (all of them when split == 1)
+    const int k = gw / split, sub = gw - k * split;
     if (lane < 16) s_vp[lane] = P.vp[(long long)k * 16 + lane];
 
     // ---- K1: instance table, flattened over nodes in draw order ---------
@@ -221,7 +224,7 @@ __global__ void __launch_bounds__(kSoftWarps * 32) soft_small_kernel(const __gri
     }
     __syncwarp();
 
-    if (!BACKWARD) {
+    if (!BACKWARD && split == 1) {
       // the whole scene as background: float4 stores per plane
       const int n4 = HW >> 2;
       float4* o4 = reinterpret_cast<float4*>(A.out + (long long)k * 3 * HW);
@@ -236,9 +239,26 @@ __global__ void __launch_bounds__(kSoftWarps * 32) soft_small_kernel(const __gri
     // ---- K3: the blocks with candidates, one pixel per lane ----------------
     for (int b0 = 0; b0 < nblocks; b0 += 32) {
       uint32_t any = 0u;
-      if (b0 + lane < nblocks)
+      const bool mine = (b0 + lane < nblocks) && ((b0 + lane) % split == sub);
+      if (mine)
         for (int w = 0; w < words; ++w) any |= bmask[(b0 + lane) * words + w];
-      uint32_t todo = __ballot_sync(0xffffffffu, any != 0u);
+      uint32_t todo = __ballot_sync(0xffffffffu, mine && any != 0u);
+      if (!BACKWARD && split > 1) {
+        // background for this warp's blocks without candidates, one pixel per lane
+        uint32_t empty = __ballot_sync(0xffffffffu, mine && any == 0u);
+        while (empty) {
+          const int b = b0 + __ffs(empty) - 1;
+          empty &= empty - 1u;
+          const int by = b / nbx, bx = b - by * nbx;
+          const int x = bx * kBlkW + lx, y = by * kBlkH + ly;
+          if (x < W && y < H) {
+            float* o = A.out + (long long)k * 3 * HW + y * W + x;
+            o[0] = P.bg[0];
+            o[HW] = P.bg[1];
+            o[2 * HW] = P.bg[2];
+          }
+        }
+      }
       while (todo) {
         const int b = b0 + __ffs(todo) - 1;
         todo &= todo - 1u;

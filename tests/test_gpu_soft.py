@@ -165,12 +165,12 @@ def test_soft_step_and_optimisation(cuda):
     assert losses[-1] < 0.5 * losses[0], losses
 
 
-def test_soft_warp_and_tile_kernels_agree(cuda):
+@pytest.mark.parametrize("n", [6, 2600])
+def test_soft_warp_and_tile_kernels_agree(cuda, n):
     """The scene-per-warp soft kernels (forward and adjoint) against the tile
     kernels on the same CartPole scenes: same model, different work layout
-    and summation order.  Forward within 1e-6, gradients within 1e-5
-    (norm-wise relative)."""
-    n = 6
+    and summation order.  6 scenes run several warps per scene, 2600 scenes
+    one.  Forward within 1e-6, gradients within 1e-5 (norm-wise relative)."""
     st = workloads.cartpole_states(n, seed=41, device=cuda)
     target = torch.rand((n, 3, 64, 64), generator=torch.Generator().manual_seed(42)).to(cuda) * 0.3
     res = {}

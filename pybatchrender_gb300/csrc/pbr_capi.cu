@@ -137,13 +137,10 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
     max_inst_verts = std::max(max_inst_verts, (long long)nd.ips * me.nv);
     if (me.smooth) A.smooth_any = 1;
   }
-  A.vcap = std::max(max_nv, (int)std::min<long long>(max_inst_verts, 1024));
-  A.vcap = (A.vcap + 31) & ~31;
+  // no vertex cache: each thread transforms its own triangle's vertices
+  A.vcap = 0;
   int icap = 1;
-  for (int n = n0; n < n1; ++n) {
-    const NodeDesc& nd = P.nodes[n];
-    icap = std::max(icap, std::min(nd.ips, A.vcap / std::max(1, P.meshes[nd.mesh].nv)));
-  }
+  for (int n = n0; n < n1; ++n) icap = std::max(icap, P.nodes[n].ips);
   A.icap = std::min(icap, 256);
   const long long need = 2 * scene_source_tris(ctx, n0, n1);
   int cap = tri_cap_req > 0 ? tri_cap_req : (int)std::min<long long>(std::max<long long>(need, 64), 1024);
@@ -165,9 +162,8 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
       cap = std::max(64, (cap / 2 + 31) & ~31);
       continue;
     }
-    if (A.vcap > max_nv) {
-      A.vcap = std::max(max_nv, A.vcap / 2);
-      A.icap = std::max(1, std::min(A.icap, A.vcap / max_nv));
+    if (A.icap > 32) {
+      A.icap = std::max(32, A.icap / 2);
       continue;
     }
     return set_err(ctx, PBR_ERR_CAPACITY,

@@ -5,25 +5,32 @@
 // for 64x64 at 256 threads).  Per item the CTA runs the whole pipeline in
 // shared memory, with no global scratch:
 //
-//   K1  instance + vertex stage: per instance M = [R(hpr)*s | t]
-//       (renderer/shader_context.py:47-84, renderer/node.py:116-126), then
-//       clip = VP[k] * M * v and n = normalize(mat3(M) n)  (shaders/basic.vert:29-53)
-//   K2  triangle setup: near-plane clip, GL viewport transform into the scene's
-//       own image (basic.vert:45-52 + the atlas flip of renderer/frame_grabber.py:105),
-//       back-face cull, bbox, watertight FP32 edge functions with the top-left
-//       rule, depth plane, flat shading resolved per triangle; survivors are
-//       compacted in draw order with a block prefix sum into a shared-memory
-//       triangle list ("chunk")
+//   K1  instance stage: per instance M = [R(hpr)*s | t]
+//       (renderer/shader_context.py:47-84, renderer/node.py:116-126), in
+//       batches of up to icap instances
+//   K2  one source triangle per thread: its three vertices clip = VP[k] * M * v
+//       (shaders/basic.vert:29-53), near-plane clip, GL viewport transform into
+//       the scene's own image (basic.vert:45-52 + the atlas flip of
+//       renderer/frame_grabber.py:105), back-face cull, bbox; survivors get
+//       their world normal(s), watertight FP32 edge functions with the
+//       top-left rule, depth plane and flat shading, and are compacted in draw
+//       order (warp prefix sums + per-warp totals, one barrier per round) into
+//       a shared-memory triangle list ("chunk")
 //       + warp-ballot binner: one __ballot_sync per (32 triangles, bin) builds
 //       the per-bin triangle bit masks
-//   K3  tile raster: every lane owns 16 consecutive pixels, iterates the set
-//       bits of its warp's bins in ascending (= draw) order, depth-tests
-//       strict-less, then resolves the winner's colour (basic.frag:20-39) and
-//       writes each channel with one 128-bit store straight into the
-//       [N,C,H,W] output (no framebuffer, no readback, no rearrange copy).
+//   K3  raster of the chunk, bin by bin (warps take bins in turn): the
+//       candidates' (triangle, pixel) pairs inside the bin are packed 32 per
+//       pass (prefix sum of the clipped bbox areas), so tiny triangles cost a
+//       few instructions each; every covered pixel does a 64-bit atomicMin of
+//       (window depth, emit order + 1) into the region's key array in shared
+//       memory -- strict-less depth, ties to the earlier drawn triangle, across
+//       chunks; then each lane resolves the colours of its 16 pixels that the
+//       chunk won (basic.frag:20-39) and, after the last chunk, writes each
+//       channel with one 128-bit store straight into the [N,C,H,W] output (no
+//       framebuffer, no readback, no rearrange copy).
 //
-// Scenes whose triangles overflow the chunk are processed chunk by chunk with
-// the per-pixel depth/colour kept in shared memory between chunks.
+// Scenes whose triangles overflow the chunk are processed chunk by chunk; the
+// key array and the per-lane colours carry over between chunks.
 #include <cstdio>
 
 #include "pbr_device.cuh"
@@ -31,36 +38,8 @@
 
 namespace pbr {
 
-template <int THREADS>
-__device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp, int& total) {
-  constexpr int NW = THREADS / 32;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) s_warp[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    int w = lane < NW ? s_warp[lane] : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
-    }
-    if (lane < NW) s_warp[lane] = w;
-  }
-  __syncthreads();
-  const int prefix = warp > 0 ? s_warp[warp - 1] : 0;
-  total = s_warp[NW - 1];
-  __syncthreads();
-  return prefix + x - v;
-}
-
 template <int THREADS, bool PLAIN, bool WINNER>
-__global__ void __launch_bounds__(THREADS) hard_kernel(const __grid_constant__ SceneParams P,
+__global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __grid_constant__ SceneParams P,
                                                        const __grid_constant__ RasterArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int NW = THREADS / 32;
@@ -79,13 +58,10 @@ __global__ void __launch_bounds__(THREADS) hard_kernel(const __grid_constant__ S
   S.H = (float)P.H;
   S.cull = P.cull;
   uint32_t* masks = reinterpret_cast<uint32_t*>(smem + L.masks);
-  float4* vcache = reinterpret_cast<float4*>(smem + L.vcache);
   float4* icache = reinterpret_cast<float4*>(smem + L.icache);
-  float* st_z = reinterpret_cast<float*>(smem + L.state);
-  uint32_t* st_c = reinterpret_cast<uint32_t*>(smem + L.state) + THREADS * kPx;
-  int32_t* st_w = reinterpret_cast<int32_t*>(smem + L.state) + 2 * THREADS * kPx;
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem + L.state);  // [THREADS * kPx]
   int* s_scan = reinterpret_cast<int*>(smem + L.misc);
-  float* s_vp = reinterpret_cast<float*>(s_scan + NW + 8);
+  float* s_vp = reinterpret_cast<float*>(s_scan + 2 * NW + 8);
   int* s_item = reinterpret_cast<int*>(s_vp + 16);
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -118,17 +94,33 @@ __global__ void __launch_bounds__(THREADS) hard_kernel(const __grid_constant__ S
     // this thread's 16 pixels: flat indices q0 .. q0+15 of the region
     const int q0 = p0 + tid * kPx;
     const int ly = q0 / W, lx = q0 - ly * W;
-    const int lane_y1 = min((q0 + kPx - 1) / W, H - 1);
-    const int lane_x0 = (lane_y1 == ly) ? lx : 0;
-    const int lane_x1 = (lane_y1 == ly) ? lx + kPx - 1 : W - 1;
     const bool active = q0 < p1;
 
-    float zb[kPx];
-    int win[kPx];
-    int nflush = 0;
+    // Per-pixel state of the region across chunks.  keys[q - p0] (shared
+    // memory) = depth bits << 32 | (emit order + 1), where emit order counts
+    // the triangles of earlier chunks too: atomicMin keeps the nearest
+    // fragment and, for equal depths, the earliest drawn (order 0 = the
+    // buffer's previous content).  The colour (and winner id) of each of this
+    // lane's 16 pixels stay in registers and are updated after every chunk
+    // for the pixels that chunk won.
+    uint32_t col[kPx];
+    int32_t wid[kPx];
     int tri_count = 0;
+    unsigned emit_base = 0;  // triangles emitted by earlier chunks
+#pragma unroll
+    for (int j = 0; j < kPx; ++j) {
+      const int q = q0 + j;
+      unsigned long long k0 = (unsigned long long)__float_as_uint(1.f) << 32;
+      col[j] = P.bg_packed;
+      if (PLAIN && q < p1) {
+        k0 = (unsigned long long)(__float_as_uint(A.zbuf[(long long)k * HW + q]) & 0x7fffffffu) << 32;
+        col[j] = A.cbuf[(long long)k * HW + q];
+      }
+      keys[tid * kPx + j] = k0;
+      wid[j] = -1;
+    }
 
-    // ---- K3 + resolve for the current chunk ------------------------------
+    // ---- K3: pixel-pair raster of the current chunk, then resolve ---------
     auto flush = [&](bool final_flush) {
       const int T = tri_count;
       const int nw = (T + 31) >> 5;
@@ -156,107 +148,87 @@ __global__ void __launch_bounds__(THREADS) hard_kernel(const __grid_constant__ S
             if (lane == 0) masks[(by * A.bins_x + bx) * words + w] = m;
           }
       }
-      // pixel state in
-#pragma unroll
-      for (int j = 0; j < kPx; ++j) {
-        win[j] = -1;
-        if (nflush == 0) {
-          if (PLAIN) {
-            const int q = q0 + j;
-            zb[j] = (q < p1) ? A.zbuf[(long long)k * HW + q] : 1.f;
-          } else {
-            zb[j] = 1.f;
-          }
-        } else {
-          zb[j] = st_z[j * THREADS + tid];
-        }
-      }
       __syncthreads();
-      // the warp's bins: rows of its 32*16 pixels, columns it touches
-      const int wq0 = p0 + warp * 32 * kPx;
-      const int wq1 = min(wq0 + 32 * kPx, p1) - 1;
-      int wbx0 = 0, wbx1 = -1, wby0 = 0, wby1 = -1;
-      if (wq0 < p1) {
-        const int wy0 = wq0 / W, wy1 = wq1 / W;
-        wby0 = wy0 / B - by_lo;
-        wby1 = wy1 / B - by_lo;
-        if (wy0 == wy1) {
-          wbx0 = (wq0 - wy0 * W) / B;
-          wbx1 = (wq1 - wy1 * W) / B;
-        } else {
-          wbx0 = 0;
-          wbx1 = A.bins_x - 1;
-        }
-      }
-      const int wnbx = wbx1 - wbx0 + 1;
-      const int wnb = (wby1 >= wby0) ? (wby1 - wby0 + 1) * wnbx : 0;
-      const float py_a = (float)ly + 0.5f;
-      for (int w = 0; w < nw; ++w) {
-        uint32_t m = 0u;
-        for (int b = lane; b < wnb; b += 32) {
-          const int by = wby0 + b / wnbx, bx = wbx0 + b % wnbx;
-          m |= masks[(by * A.bins_x + bx) * words + w];
-        }
-        m = __reduce_or_sync(0xffffffffu, m);
-        while (m) {
-          const int j0 = __ffs(m) - 1;
-          m &= m - 1u;
-          const int t = w * 32 + j0;
-          const float4 zp = S.T3[t];
-          const float4 meta = S.T4[t];
-          const uint32_t xb = __float_as_uint(zp.w), yb = __float_as_uint(meta.x);
-          const int tx0 = (int)(xb & 0xffffu), tx1 = (int)(xb >> 16);
-          const int ty0 = (int)(yb & 0xffffu), ty1 = (int)(yb >> 16);
-          if (!active || ty1 < ly || ty0 > lane_y1 || tx1 < lane_x0 || tx0 > lane_x1) continue;
-          const float4 e0 = S.T0[t], e1 = S.T1[t], e2 = S.T2[t];
-          const uint32_t fl = __float_as_uint(meta.y);
-          const bool tl0 = fl & 1u, tl1 = fl & 2u, tl2 = fl & 4u;
+      // bins warp-strided; per bin and mask word, the candidates' (triangle, pixel)
+      // pairs inside the bin are packed 32 per pass (prefix sum of the clipped bbox areas)
+      for (int b = warp; b < nbins; b += NW) {
+        const int bry = b / A.bins_x, bcx = b - bry * A.bins_x;
+        const int bx0 = bcx * B, bx1 = min(bx0 + B, W) - 1;
+        const int by0 = max((by_lo + bry) * B, ry0), by1 = min((by_lo + bry) * B + B - 1, ry1);
+        for (int w = 0; w < nw; ++w) {
+          const uint32_t m = masks[b * words + w];
+          if (m == 0u) continue;
+          int ax0 = 0, ay0 = 0, bw = 1, npx = 0;
+          if ((m >> lane) & 1u) {
+            const int t = w * 32 + lane;
+            const uint32_t xb = __float_as_uint(S.T3[t].w), yb = __float_as_uint(S.T4[t].x);
+            ax0 = max((int)(xb & 0xffffu), bx0);
+            const int ax1 = min((int)(xb >> 16), bx1);
+            ay0 = max((int)(yb & 0xffffu), by0);
+            const int ay1 = min((int)(yb >> 16), by1);
+            const int bh = ay1 - ay0 + 1;
+            bw = ax1 - ax0 + 1;
+            npx = (bw > 0 && bh > 0) ? bw * bh : 0;
+            bw = max(bw, 1);
+          }
+          const float ibw = __fdividef(1.f, (float)bw);
+          int incl = npx;
 #pragma unroll
-          for (int j = 0; j < kPx; ++j) {
-            int x = lx + j;
-            float py = py_a;
-            if (x >= W) {
-              x -= W;
-              py += 1.f;
-              while (x >= W) { x -= W; py += 1.f; }
+          for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+          }
+          const int total = __shfl_sync(0xffffffffu, incl, 31);
+          for (int g0 = 0; g0 < total; g0 += 32) {
+            const int g = g0 + lane;
+            int o = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+              const int probe = __shfl_sync(0xffffffffu, incl, o + step - 1);
+              if (probe <= g) o += step;
             }
-            const float px = (float)x + 0.5f;
+            const int o_start = __shfl_sync(0xffffffffu, incl - npx, o);
+            const int o_ax0 = __shfl_sync(0xffffffffu, ax0, o);
+            const int o_ay0 = __shfl_sync(0xffffffffu, ay0, o);
+            const int o_bw = __shfl_sync(0xffffffffu, bw, o);
+            const float o_ibw = __shfl_sync(0xffffffffu, ibw, o);
+            if (g >= total) continue;
+            const int t = w * 32 + o;
+            const int local = g - o_start;
+            // (local + 0.5) / bw lies at least 0.5 / bw >= 1/64 from an integer
+            const int ry = (int)(((float)local + 0.5f) * o_ibw);
+            const int xx = o_ax0 + local - ry * o_bw, yy = o_ay0 + ry;
+            const int q = yy * W + xx;
+            if (q < p0 || q >= p1) continue;  // the region starts or ends inside a row
+            const float px = (float)xx + 0.5f, py = (float)yy + 0.5f;
+            const float4 e0 = S.T0[t], e1 = S.T1[t], e2 = S.T2[t], zp = S.T3[t];
+            const uint32_t fl = __float_as_uint(S.T4[t].y);
             const float E0 = fmaf(e0.x, px - e0.z, e0.y * (py - e0.w));
             const float E1 = fmaf(e1.x, px - e1.z, e1.y * (py - e1.w));
             const float E2 = fmaf(e2.x, px - e2.z, e2.y * (py - e2.w));
-            const bool in0 = tl0 ? (E0 >= 0.f) : (E0 > 0.f);
-            const bool in1 = tl1 ? (E1 >= 0.f) : (E1 > 0.f);
-            const bool in2 = tl2 ? (E2 >= 0.f) : (E2 > 0.f);
-            const float z = fmaxf(fmaf(zp.x, px, fmaf(zp.y, py, zp.z)), 0.f);
-            if (in0 && in1 && in2 && z < zb[j] && q0 + j < p1) {
-              zb[j] = z;
-              win[j] = t;
+            const bool in0 = (fl & 1u) ? (E0 >= 0.f) : (E0 > 0.f);
+            const bool in1 = (fl & 2u) ? (E1 >= 0.f) : (E1 > 0.f);
+            const bool in2 = (fl & 4u) ? (E2 >= 0.f) : (E2 > 0.f);
+            if (in0 && in1 && in2) {
+              const float z = fmaxf(fmaf(zp.x, px, fmaf(zp.y, py, zp.z)), 0.f);
+              // z >= 0, so its bits order like the values (the mask folds -0 into +0)
+              const unsigned long long key = ((unsigned long long)(__float_as_uint(z) & 0x7fffffffu) << 32) |
+                                             (unsigned)(emit_base + (unsigned)t + 1u);
+              atomicMin(&keys[q - p0], key);
             }
           }
         }
       }
-      // resolve winners of this chunk
-      uint32_t col[kPx];
-      int32_t wid[kPx];
+      __syncthreads();
+      // resolve the pixels this chunk won
+      const float py_a = (float)ly + 0.5f;
 #pragma unroll
       for (int j = 0; j < kPx; ++j) {
-        if (nflush == 0) {
-          if (PLAIN) {
-            const int q = q0 + j;
-            col[j] = (q < p1) ? A.cbuf[(long long)k * HW + q] : P.bg_packed;
-          } else {
-            col[j] = P.bg_packed;
-          }
-          wid[j] = -1;
-        } else {
-          col[j] = st_c[j * THREADS + tid];
-          if (WINNER) wid[j] = st_w[j * THREADS + tid];
-        }
-        if (win[j] >= 0) {
-          const int t = win[j];
+        const uint32_t lo = (uint32_t)keys[tid * kPx + j];
+        if (q0 + j < p1 && lo > emit_base) {
+          const int t = (int)(lo - emit_base) - 1;
           const float4 meta = S.T4[t];
-          const uint32_t fl = __float_as_uint(meta.y);
-          if (fl & 8u) {
+          if (__float_as_uint(meta.y) & 8u) {
             int x = lx + j;
             float py = py_a;
             while (x >= W) { x -= W; py += 1.f; }
@@ -267,15 +239,12 @@ __global__ void __launch_bounds__(THREADS) hard_kernel(const __grid_constant__ S
           if (WINNER) wid[j] = __float_as_int(meta.w);
         }
       }
-      if (!final_flush) {
-#pragma unroll
-        for (int j = 0; j < kPx; ++j) {
-          st_z[j * THREADS + tid] = zb[j];
-          st_c[j * THREADS + tid] = col[j];
-          if (WINNER) st_w[j * THREADS + tid] = wid[j];
-        }
-      } else if (active) {
+      emit_base += (unsigned)T;
+      if (final_flush && active) {
         const bool full = (q0 + kPx <= p1);
+        float zb[kPx];
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) zb[j] = __uint_as_float((uint32_t)(keys[tid * kPx + j] >> 32));
         if (PLAIN) {
           float* zdst = A.zbuf + (long long)k * HW + q0;
           uint32_t* cdst = A.cbuf + (long long)k * HW + q0;
@@ -321,29 +290,34 @@ __global__ void __launch_bounds__(THREADS) hard_kernel(const __grid_constant__ S
           }
         }
       }
-      ++nflush;
       tri_count = 0;
       __syncthreads();
     };
 
     // ---- K1 / K2: walk nodes and instances in draw order -----------------
+    // Instance batches of up to icap instances (model matrices in shared
+    // memory); then rounds of THREADS source triangles, one per thread: the
+    // thread transforms its triangle's three vertices itself (no vertex cache,
+    // no per-instance barriers), culls and rejects triangles that cover no
+    // pixel centre, and the survivors are compacted in draw order with one
+    // barrier per round (warp prefix sums + per-warp totals in shared memory).
     __syncthreads();  // s_vp visible
     const float vp0 = s_vp[0], vp1 = s_vp[1], vp2 = s_vp[2], vp3 = s_vp[3];
     const float vp4 = s_vp[4], vp5 = s_vp[5], vp6 = s_vp[6], vp7 = s_vp[7];
     const float vp8 = s_vp[8], vp9 = s_vp[9], vp10 = s_vp[10], vp11 = s_vp[11];
     const float vp12 = s_vp[12], vp13 = s_vp[13], vp14 = s_vp[14], vp15 = s_vp[15];
+    int parity = 0;
     for (int n = A.node_begin; n < A.node_end; ++n) {
       const NodeDesc& nd = P.nodes[n];
       const MeshDesc& me = P.meshes[nd.mesh];
       int cnt = nd.counts ? nd.counts[k] : nd.ips;
       cnt = max(0, min(cnt, nd.ips));
-      const int nv = me.nv, nt = me.nt;
+      const int nt = me.nt;
       if (cnt == 0 || nt == 0) continue;
-      const int nb = max(1, min(A.icap, A.vcap / nv));
       const bool smooth = me.smooth != 0;
-      for (int b0 = 0; b0 < cnt; b0 += nb) {
-        const int nbc = min(nb, cnt - b0);
-        // instance stage
+      for (int b0 = 0; b0 < cnt; b0 += A.icap) {
+        const int nbc = min(A.icap, cnt - b0);
+        __syncthreads();  // the previous batch's triangles are done with icache
         for (int i = tid; i < nbc; i += THREADS) {
           const long long id = nd.shared ? (long long)(b0 + i) : (long long)k * nd.ips + b0 + i;
           float m[12];
@@ -356,52 +330,94 @@ __global__ void __launch_bounds__(THREADS) hard_kernel(const __grid_constant__ S
           icache[i * 4 + 3] = make_float4(cc[0], cc[1], cc[2], cc[3]);
         }
         __syncthreads();
-        // vertex stage
-        for (int v = tid; v < nbc * nv; v += THREADS) {
-          const int li = v / nv, vi = v - li * nv;
-          const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
-          const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
-          const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
-          const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
-          const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
-          float4 c;
-          c.x = vp0 * wx + vp1 * wy + vp2 * wz + vp3;
-          c.y = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
-          c.z = vp8 * wx + vp9 * wy + vp10 * wz + vp11;
-          c.w = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
-          const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
-          float nx = r0.x * ax + r0.y * ay + r0.z * az;
-          float ny = r1.x * ax + r1.y * ay + r1.z * az;
-          float nz = r2.x * ax + r2.y * ay + r2.z * az;
-          const float l2 = nx * nx + ny * ny + nz * nz;
-          const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
-          vcache[2 * v] = c;
-          vcache[2 * v + 1] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
-        }
-        __syncthreads();
-        // triangle stage, rounds of RT source triangles
         const int total_t = nbc * nt;
         for (int t0 = 0; t0 < total_t; t0 += RT) {
+          // up to 2 emitted triangles per source triangle (near-plane clip)
           const int rem = min(RT, total_t - t0);
           if (tri_count + 2 * rem > A.tri_cap) flush(false);
-          int c = 0, li = 0, ti = 0;
-          const bool mine = tid < rem;
-          if (mine) {
+          int c = 0, li = 0, ti = 0, i0 = 0, i1 = 0, i2 = 0;
+          float4 cv[3];
+          SV sv[3];
+          bool front = false;
+          if (tid < rem) {
             const int t = t0 + tid;
             li = t / nt;
             ti = t - li * nt;
-            c = process_tri<false>(P, S, vcache, li * nv, me.idx[3 * ti], me.idx[3 * ti + 1], me.idx[3 * ti + 2], 0,
-                                   icache[li * 4 + 3], 0, smooth);
+            i0 = me.idx[3 * ti];
+            i1 = me.idx[3 * ti + 1];
+            i2 = me.idx[3 * ti + 2];
+            const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
+            const int iv[3] = {i0, i1, i2};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const int vi = iv[q];
+              const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
+              const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
+              const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
+              const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
+              cv[q].x = vp0 * wx + vp1 * wy + vp2 * wz + vp3;
+              cv[q].y = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
+              cv[q].z = vp8 * wx + vp9 * wy + vp10 * wz + vp11;
+              cv[q].w = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
+            }
+            const float d0 = cv[0].z + cv[0].w, d1 = cv[1].z + cv[1].w, d2 = cv[2].z + cv[2].w;
+            front = d0 >= 0.f && d1 >= 0.f && d2 >= 0.f;
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (front) {
+#pragma unroll
+              for (int q = 0; q < 3; ++q) sv[q] = to_screen(cv[q], S.W, S.H);
+              c = setup_tri_sv<false>(P, S, sv[0], z4, sv[1], z4, sv[2], z4, 0, z4, 0, smooth);
+            } else if (!(d0 < 0.f && d1 < 0.f && d2 < 0.f)) {
+              c = clip_tri<false>(P, S, cv[0], z4, cv[1], z4, cv[2], z4, i0, i1, i2, 0, z4, 0, smooth);
+            }
           }
-          int total;
-          const int off = block_exclusive_scan<THREADS>(c, s_scan, total);
+          // draw-order compaction: warp prefix sum, then the totals of the warps before this one
+          int incl = c;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          int* wcnt = s_scan + parity * NW;
+          if (lane == 31) wcnt[warp] = incl;
+          __syncthreads();
+          int before = 0, total = 0;
+#pragma unroll
+          for (int w = 0; w < NW; ++w) {
+            const int v = wcnt[w];
+            before += w < warp ? v : 0;
+            total += v;
+          }
+          parity ^= 1;
           if (c > 0) {
+            const int slot = tri_count + before + incl - c;
+            const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
+            const float4 col = icache[li * 4 + 3];
             const int draw_id = (nd.rank_base + b0 + li) * P.max_tris + ti;
-            process_tri<true>(P, S, vcache, li * nv, me.idx[3 * ti], me.idx[3 * ti + 1], me.idx[3 * ti + 2],
-                              tri_count + off, icache[li * 4 + 3], draw_id, smooth);
+            // world normals: the provoking vertex's for flat meshes (the three are identical), all three if smooth
+            float4 nv[3];
+            const int iv[3] = {i0, i1, i2};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              if (q == 0 || smooth) {
+                const int vi = iv[q];
+                const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
+                const float nx = r0.x * ax + r0.y * ay + r0.z * az;
+                const float ny = r1.x * ax + r1.y * ay + r1.z * az;
+                const float nz = r2.x * ax + r2.y * ay + r2.z * az;
+                const float l2 = nx * nx + ny * ny + nz * nz;
+                const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
+                nv[q] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
+              } else {
+                nv[q] = nv[0];
+              }
+            }
+            if (front)
+              setup_tri_sv<true>(P, S, sv[0], nv[0], sv[1], nv[1], sv[2], nv[2], slot, col, draw_id, smooth);
+            else
+              clip_tri<true>(P, S, cv[0], nv[0], cv[1], nv[1], cv[2], nv[2], i0, i1, i2, slot, col, draw_id, smooth);
           }
           tri_count += total;
-          __syncthreads();
         }
       }
     }

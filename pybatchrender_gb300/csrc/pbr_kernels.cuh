@@ -110,8 +110,8 @@ struct SmemLayout {
   int masks;               // uint32 [max_region_bins * tri_cap/32]
   int vcache;              // float4 [vcap*2]: clip position, world normal
   int icache;              // float4 [icap*4]: model matrix rows, colour
-  int state;               // per-pixel state across chunks [kPx][threads] (z, rgba, id)
-  int misc;                // scan scratch, VP, work item
+  int state;               // per-pixel depth / emit-order keys of the region [threads*kPx] (uint64)
+  int misc;                // per-warp survivor counts (two rounds), VP, work item
   int total;
 };
 
@@ -137,13 +137,9 @@ __host__ __device__ inline SmemLayout smem_layout(const RasterArgs& a, int threa
   L.masks = off; off += align16(a.max_region_bins * (a.tri_cap / 32) * 4);
   L.vcache = off; off += align16(a.vcap * 32);
   L.icache = off; off += align16(a.icap * 64);
-  if (a.multi_chunk) {
-    L.state = off;
-    off += align16(threads * kPx * (winner ? 12 : 8));
-  } else {
-    L.state = 0;
-  }
-  L.misc = off; off += align16((threads / 32 + 8) * 4 + 16 * 4 + 16);
+  L.state = off;  // depth / emit-order keys of the region's pixels, uint64 each
+  off += align16(threads * kPx * 8);
+  L.misc = off; off += align16((2 * (threads / 32) + 8) * 4 + 16 * 4 + 16);
   L.total = off;
   return L;
 }

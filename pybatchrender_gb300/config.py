@@ -71,6 +71,7 @@ class PBRConfig:
     raster_method: str = 'batched'   # 'batched' (one fused launch) | 'plain' (per-node launches, host-built matrices)
     raster_mode: str = 'hard'        # 'hard' (uint8 pixels) | 'soft' (float32, differentiable)
     raster_kernel: str = 'auto'      # 'auto' | 'warp' (scene per warp, small scenes) | 'tile' (CTA per region)
+                                     # | 'binned' (soft mode: global per-block candidate masks, large scenes)
     raster_threads: int = 256        # threads per CTA: 128 | 256 | 512
     bin_size: int = 16               # binner tile size in pixels: 8 | 16 | 32
     tri_cap: int = 0                 # triangles per shared-memory chunk (0 = automatic)
@@ -164,8 +165,8 @@ class PBRConfig:
             raise ValueError(f"raster_method must be 'batched' or 'plain', got {self.raster_method!r}")
         if self.raster_mode not in ('hard', 'soft'):
             raise ValueError(f"raster_mode must be 'hard' or 'soft', got {self.raster_mode!r}")
-        if self.raster_kernel not in ('auto', 'warp', 'tile'):
-            raise ValueError("raster_kernel must be 'auto', 'warp' or 'tile'")
+        if self.raster_kernel not in ('auto', 'warp', 'tile', 'binned'):
+            raise ValueError("raster_kernel must be 'auto', 'warp', 'tile' or 'binned'")
         if self.raster_threads not in (128, 256, 512):
             raise ValueError("raster_threads must be 128, 256 or 512")
         if self.bin_size not in (8, 16, 32):

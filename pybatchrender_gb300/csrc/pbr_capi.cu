@@ -34,7 +34,7 @@ struct pbr_ctx {
   int bin_px = 16;
   int tri_cap_req = 0;
   int persistent = 0;
-  int kernel = 0;  // 0 auto, 1 scene-per-warp, 2 tile (CTA per scene region)
+  int kernel = 0;  // 0 auto, 1 scene-per-warp, 2 tile (CTA per scene region), 3 binned (soft only)
   // scratch
   int32_t* d_counter = nullptr;
   int32_t* d_status = nullptr;
@@ -44,6 +44,9 @@ struct pbr_ctx {
   int smem_set[3][2][2] = {};
   int small_smem_set[2][2][2] = {};
   int soft_small_smem_set[2] = {};
+  int soft_large_smem_set[2] = {};
+  float4* d_soft_scratch = nullptr;  // binned soft kernel slabs, grown on demand
+  size_t soft_scratch_bytes = 0;
   int soft_smem_set[2][2] = {};
   int soft_threads = 256;
 };
@@ -332,6 +335,7 @@ int pbr_destroy(pbr_ctx* ctx) {
   cudaFree(ctx->d_counter);
   cudaFree(ctx->d_zbuf);
   cudaFree(ctx->d_cbuf);
+  cudaFree(ctx->d_soft_scratch);
   delete ctx;
   return PBR_OK;
 }
@@ -478,7 +482,8 @@ int pbr_background_set(pbr_ctx* ctx, const float rgba[4]) {
 
 int pbr_raster_config(pbr_ctx* ctx, int kernel, int threads, int bin_px, int tri_cap, int persistent) {
   PBR_CHECK_CTX(ctx);
-  if (kernel < 0 || kernel > 2) return set_err(ctx, PBR_ERR_INVALID, "kernel must be 0 (auto), 1 or 2 (got %d)", kernel);
+  if (kernel < 0 || kernel > 3)
+    return set_err(ctx, PBR_ERR_INVALID, "kernel must be 0 (auto), 1, 2 or 3 (got %d)", kernel);
   if (threads != 128 && threads != 256 && threads != 512)
     return set_err(ctx, PBR_ERR_INVALID, "threads must be 128, 256 or 512 (got %d)", threads);
   if (bin_px != 8 && bin_px != 16 && bin_px != 32)
@@ -761,15 +766,81 @@ static int plan_soft_small(pbr_ctx* ctx, bool backward, pbr::SoftArgs* out, int*
   return PBR_OK;
 }
 
-// Soft kernel choice, identical for both passes: 1 = scene per warp, 2 = tile.
+// Binned soft plan (both passes): persistent CTAs, one slab of scratch each,
+// sized for the scene's source triangles.  Allocates the slabs on first use
+// (and when a larger scene needs more).
+static int plan_soft_large(pbr_ctx* ctx, bool backward, pbr::SoftArgs* out, int* smem_out, int* grid_out) {
+  const SceneParams& P = ctx->P;
+  long long tris = 0, insts = 0;
+  int max_ips = 1;
+  for (int n = 0; n < P.num_nodes; ++n) {
+    const NodeDesc& nd = P.nodes[n];
+    tris += (long long)nd.ips * P.meshes[nd.mesh].nt;
+    insts += nd.ips;
+    max_ips = std::max(max_ips, nd.ips);
+  }
+  if (tris > (1 << 22)) return set_err(ctx, PBR_ERR_CAPACITY, "binned soft kernel: at most 4M triangles per scene");
+  if (insts > 1024)
+    return set_err(ctx, PBR_ERR_CAPACITY, "soft mode supports at most 1024 instances per scene (got %lld)", insts);
+  pbr::SoftArgs A;
+  memset(&A, 0, sizeof(A));
+  A.tri_cap = (int)std::max<long long>(32, (tris + 31) & ~31LL);
+  A.icap = std::min(max_ips, 256);
+  A.iacc_cap = (int)std::max<long long>(1, insts);
+  A.backward = backward ? 1 : 0;
+  A.num_items = P.N;
+  A.status = ctx->d_status;
+  const int smem = pbr::soft_large_smem_bytes(A);
+  // both passes share the slabs (one per CTA): size them for the larger grid of the two
+  int grid = 1, grid_max = 1;
+  for (int pass = 0; pass < 2; ++pass) {
+    pbr::SoftArgs Ap = A;
+    Ap.backward = pass;
+    const int smem_p = pbr::soft_large_smem_bytes(Ap);
+    if (smem_p > ctx->max_smem) return set_err(ctx, PBR_ERR_CAPACITY, "binned soft layout exceeds shared memory");
+    int& cached = ctx->soft_large_smem_set[pass];
+    if (smem_p > 48 * 1024 && smem_p > cached) {
+      cudaError_t ea = pbr::soft_large_set_smem_limit(pass == 1, smem_p);
+      if (ea != cudaSuccess) return cuda_err(ctx, ea, "cudaFuncSetAttribute");
+      cached = smem_p;
+    }
+    int bps = 1;
+    cudaError_t e = pbr::soft_large_occupancy(pass == 1, smem_p, &bps);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "occupancy");
+    const int g = std::max(1, std::min(P.N, ctx->sm_count * std::max(1, bps)));
+    grid_max = std::max(grid_max, g);
+    if ((pass == 1) == backward) grid = g;
+  }
+  const int nblocks = ((P.W + 7) / 8) * ((P.H + 3) / 4);
+  const long long slab = pbr::soft_large_slab_float4(A.tri_cap, nblocks);
+  const size_t need = (size_t)slab * 16 * (size_t)grid_max;
+  cudaError_t e;
+  if (need > ctx->soft_scratch_bytes) {
+    if (ctx->d_soft_scratch) cudaFree(ctx->d_soft_scratch);
+    ctx->d_soft_scratch = nullptr;
+    ctx->soft_scratch_bytes = 0;
+    e = cudaMalloc(&ctx->d_soft_scratch, need);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaMalloc (binned soft scratch)");
+    ctx->soft_scratch_bytes = need;
+  }
+  A.scratch = ctx->d_soft_scratch;
+  A.scratch_stride = slab;
+  *out = A;
+  *smem_out = smem;
+  *grid_out = grid;
+  return PBR_OK;
+}
+
+// Soft kernel choice, identical for both passes: 1 = scene per warp, 2 = tile, 3 = binned.
 static int soft_kind(pbr_ctx* ctx) {
   if (ctx->kernel == 2) return 2;
+  if (ctx->kernel == 3) return 3;
   pbr::SoftArgs A;
   int smem = 0, grid = 0;
   if (plan_soft_small(ctx, true, &A, &smem, &grid) == PBR_OK) return 1;
   if (ctx->kernel == 1) return -1;
   ctx->err.clear();
-  return 2;
+  return 3;
 }
 
 int pbr_soft_config(pbr_ctx* ctx, float sigma, float gamma, int threads) {
@@ -805,13 +876,15 @@ int pbr_render_soft(pbr_ctx* ctx, float* d_out, float* d_stats, void* stream) {
   if (kind < 0) return PBR_ERR_CAPACITY;
   if (kind == 1 && ((uintptr_t)d_out & 15u) != 0)
     return set_err(ctx, PBR_ERR_INVALID, "d_out must be 16-byte aligned");
-  rc = kind == 1 ? plan_soft_small(ctx, false, &A, &smem, &grid)
-                 : plan_soft(ctx, ctx->soft_threads, false, &A, &smem, &grid);
+  rc = kind == 1   ? plan_soft_small(ctx, false, &A, &smem, &grid)
+       : kind == 3 ? plan_soft_large(ctx, false, &A, &smem, &grid)
+                   : plan_soft(ctx, ctx->soft_threads, false, &A, &smem, &grid);
   if (rc) return rc;
   A.out = d_out;
   A.stats = d_stats;
-  cudaError_t e = kind == 1 ? pbr::soft_small_launch(false, ctx->P, A, grid, smem, (cudaStream_t)stream)
-                            : pbr::soft_launch(ctx->soft_threads, false, ctx->P, A, grid, smem, (cudaStream_t)stream);
+  cudaError_t e = kind == 1   ? pbr::soft_small_launch(false, ctx->P, A, grid, smem, (cudaStream_t)stream)
+                  : kind == 3 ? pbr::soft_large_launch(false, ctx->P, A, grid, smem, (cudaStream_t)stream)
+                              : pbr::soft_launch(ctx->soft_threads, false, ctx->P, A, grid, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_err(ctx, e, "soft forward launch");
   return PBR_OK;
 }
@@ -831,14 +904,17 @@ int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, co
   const int kind = soft_kind(ctx);
   if (kind < 0) return PBR_ERR_CAPACITY;
   // the tile adjoint keeps 15 values per pixel in shared memory: 128-thread CTAs
-  rc = kind == 1 ? plan_soft_small(ctx, true, &A, &smem, &grid) : plan_soft(ctx, 128, true, &A, &smem, &grid);
+  rc = kind == 1   ? plan_soft_small(ctx, true, &A, &smem, &grid)
+       : kind == 3 ? plan_soft_large(ctx, true, &A, &smem, &grid)
+                   : plan_soft(ctx, 128, true, &A, &smem, &grid);
   if (rc) return rc;
   A.out = const_cast<float*>(d_out);
   A.stats = const_cast<float*>(d_stats);
   A.gout = d_grad_out;
   A.glight = d_grad_light;
-  cudaError_t e = kind == 1 ? pbr::soft_small_launch(true, ctx->P, A, grid, smem, (cudaStream_t)stream)
-                            : pbr::soft_launch(128, true, ctx->P, A, grid, smem, (cudaStream_t)stream);
+  cudaError_t e = kind == 1   ? pbr::soft_small_launch(true, ctx->P, A, grid, smem, (cudaStream_t)stream)
+                  : kind == 3 ? pbr::soft_large_launch(true, ctx->P, A, grid, smem, (cudaStream_t)stream)
+                              : pbr::soft_launch(128, true, ctx->P, A, grid, smem, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_err(ctx, e, "soft backward launch");
   return PBR_OK;
 }

@@ -96,6 +96,8 @@ struct SoftArgs {
   int32_t bin_px, bins_x, max_region_bins;
   int32_t backward;
   int32_t split;  // scene-per-warp soft kernel: warps per scene (each takes every split-th pixel block)
+  float4* scratch;          // binned soft kernel: one slab per CTA (records, block masks, accumulators)
+  int64_t scratch_stride;   // float4 per slab
 };
 
 struct SoftLayout {

@@ -32,6 +32,14 @@ int soft_small_smem_per_warp(const SoftArgs& a, int W, int H);
 cudaError_t soft_small_set_smem_limit(bool backward, int bytes);
 cudaError_t soft_small_launch(bool backward, const SceneParams& P, const SoftArgs& A, int grid, int smem_bytes,
                               cudaStream_t stream);
+// Binned soft coverage for large scenes (pbr_soft_large.cu); soft_large_threads() threads per CTA.
+int soft_large_threads();
+int soft_large_smem_bytes(const SoftArgs& a);
+long long soft_large_slab_float4(int cap, int nblocks);
+cudaError_t soft_large_set_smem_limit(bool backward, int bytes);
+cudaError_t soft_large_occupancy(bool backward, int smem_bytes, int* blocks_per_sm);
+cudaError_t soft_large_launch(bool backward, const SceneParams& P, const SoftArgs& A, int grid, int smem_bytes,
+                              cudaStream_t stream);
 cudaError_t plain_clear_launch(const SceneParams& P, float* zbuf, uint32_t* cbuf, cudaStream_t stream);
 cudaError_t plain_resolve_launch(const SceneParams& P, const float* zbuf, const uint32_t* cbuf, uint8_t* out,
                                  float* depth, cudaStream_t stream);

@@ -36,7 +36,7 @@ from .light import PBRLight
 from .node import MODE_MAT, PBRNode, mesh_key
 
 
-KERNELS = {"auto": 0, "warp": 1, "tile": 2}
+KERNELS = {"auto": 0, "warp": 1, "tile": 2, "binned": 3}
 
 
 class PBRRenderer:

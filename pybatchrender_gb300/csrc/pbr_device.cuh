@@ -149,7 +149,8 @@ template <bool WRITE>
 __device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx& S, SV v0, float4 n0, SV v1,
                                             float4 n1, SV v2, float4 n2, int slot, float4 col, int draw_id,
                                             bool smooth) {
-  float area2 = (v1.x - v0.x) * (v2.y - v0.y) - (v2.x - v0.x) * (v1.y - v0.y);
+  // one explicit fused multiply-add, so that every kernel that inlines this rounds the same way
+  float area2 = fmaf(v1.x - v0.x, v2.y - v0.y, -((v2.x - v0.x) * (v1.y - v0.y)));
   if (S.cull) {
     if (!(area2 < 0.f)) return 0;  // back-facing, degenerate or NaN
   } else {
@@ -173,9 +174,9 @@ __device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx
   const float4 e1 = make_edge(v2.x, v2.y, v0.x, v0.y, tl1);
   const float4 e2 = make_edge(v0.x, v0.y, v1.x, v1.y, tl2);
   const float ia = 1.f / area2;
-  const float zA = (e0.x * v0.z + e1.x * v1.z + e2.x * v2.z) * ia;
-  const float zB = (e0.y * v0.z + e1.y * v1.z + e2.y * v2.z) * ia;
-  const float zC = v0.z - zA * v0.x - zB * v0.y;
+  const float zA = fmaf(e2.x, v2.z, fmaf(e1.x, v1.z, e0.x * v0.z)) * ia;
+  const float zB = fmaf(e2.y, v2.z, fmaf(e1.y, v1.z, e0.y * v0.z)) * ia;
+  const float zC = fmaf(-zB, v0.y, fmaf(-zA, v0.x, v0.z));
   const uint32_t xbox = (uint32_t)fx0 | ((uint32_t)fx1 << 16);
   const uint32_t ybox = (uint32_t)fy0 | ((uint32_t)fy1 << 16);
   const uint32_t flags = (tl0 ? 1u : 0u) | (tl1 ? 2u : 0u) | (tl2 ? 4u : 0u) | (smooth ? 8u : 0u);

@@ -8,12 +8,15 @@
 //   K1  the scene's instances of every node, flattened in draw order into one
 //       table (lane = instance, so all pose loads are in flight together):
 //       model matrix M = [R(hpr)*s | t] and colour; then lane = vertex:
-//       clip = VP * M * v, n = normalize(mat3(M) n)  (shaders/basic.vert:29-53)
+//       clip = VP * M * v and its screen position (shaders/basic.vert:29-53;
+//       smooth meshes also n = normalize(mat3(M) n))
 //   K2  lane = triangle: near clip, cull, watertight edges, depth plane, flat
-//       shading; compacted in draw order with a warp prefix sum (__shfl_up);
+//       shading (a flat mesh's provoking normal is transformed here, for
+//       survivors only); compacted in draw order with a warp prefix sum;
 //       then the warp-ballot binner: for each 32x16-pixel bin one
 //       __ballot_sync over the lanes (= triangles) is the bin's mask
-//   K3  per bin: an empty bin is written as background with 128-bit stores.
+//   K3  per bin: a bin without candidates is written as background with
+//       128-bit stores.
 //       Otherwise the bin's candidate triangles and the pixels of their
 //       bbox-in-bin are laid out end to end (warp prefix sum of the areas) and
 //       dealt 32 per pass to the lanes, so many tiny triangles share a pass.
@@ -27,7 +30,7 @@
 // Shared memory per warp: the triangle list plus one region that holds the
 // vertex cache / instance table during K1-K2 and the bin's key tile during K3.
 // The host picks this kernel when a scene has at most 64 source triangles,
-// 32 instances and 256 vertices, and W % 16 == 0.
+// 32 instances, 256 vertices and 64 bins, and W % 16 == 0.
 #include "pbr_device.cuh"
 #include "pbr_launch.h"
 
@@ -314,29 +317,34 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
     }
     __syncwarp();
 
-    // ---- K3: background, then the bins that have candidates ---------------
+    // ---- K3: background for bins without candidates, raster the others -----
     uint8_t* const lane_out = A.out + (size_t)k * C * HW + lane_off;
     const size_t lane_pix = (size_t)k * HW + lane_off;
     if (!PLAIN) {
-      // the whole scene as background: coalesced 512-byte warp stores, four per trip
-      const int n16 = HW >> 4;  // uint4 per plane (HW % 16 == 0)
-      uint4* p = reinterpret_cast<uint4*>(A.out + (size_t)k * C * HW);
-      for (int c = 0; c < C; ++c, p += n16) {
-        const uint32_t v = c == 0 ? bg0 : (c == 1 ? bg1 : (c == 2 ? bg2 : bg3));
-        const uint4 v4 = make_uint4(v, v, v, v);
-        int i = lane;
-        for (; i + 96 < n16; i += 128) {
-          p[i] = v4;
-          p[i + 32] = v4;
-          p[i + 64] = v4;
-          p[i + 96] = v4;
-        }
-        for (; i < n16; i += 32) p[i] = v4;
-      }
-      if (A.depth || WINNER) {
-        for (int p = lane * 4; p < HW; p += 128) {
-          if (A.depth) *reinterpret_cast<float4*>(A.depth + (size_t)k * HW + p) = make_float4(1.f, 1.f, 1.f, 1.f);
-          if (WINNER) *reinterpret_cast<int4*>(A.winner + (size_t)k * HW + p) = make_int4(-1, -1, -1, -1);
+      // bins without candidates: background, one 128-bit store per plane (depth 1, no winner)
+      const unsigned long long row_bits = (bins_x >= 64) ? ~0ull : ((1ull << bins_x) - 1ull);
+      for (int by = 0; by < bins_y; ++by) {
+        const int row0 = by * kBinH;
+        if (row0 + seg_r >= H) continue;
+        for (unsigned long long rem = ~(ne >> (by * bins_x)) & row_bits; rem != 0ull; rem &= rem - 1ull) {
+          const int col0 = (__ffsll((long long)rem) - 1) * kBinW;
+          if (col0 + seg_x >= W) continue;
+          const int boff = row0 * W + col0;
+          uint8_t* o = lane_out + boff;
+          *reinterpret_cast<uint4*>(o) = make_uint4(bg0, bg0, bg0, bg0);
+          if (C > 1) *reinterpret_cast<uint4*>(o + HW) = make_uint4(bg1, bg1, bg1, bg1);
+          if (C > 2) *reinterpret_cast<uint4*>(o + 2 * HW) = make_uint4(bg2, bg2, bg2, bg2);
+          if (C > 3) *reinterpret_cast<uint4*>(o + 3 * HW) = make_uint4(bg3, bg3, bg3, bg3);
+          if (A.depth) {
+            float4* d = reinterpret_cast<float4*>(A.depth + lane_pix + boff);
+            const float4 one = make_float4(1.f, 1.f, 1.f, 1.f);
+            d[0] = one; d[1] = one; d[2] = one; d[3] = one;
+          }
+          if (WINNER) {
+            int4* d = reinterpret_cast<int4*>(A.winner + lane_pix + boff);
+            const int4 none = make_int4(-1, -1, -1, -1);
+            d[0] = none; d[1] = none; d[2] = none; d[3] = none;
+          }
         }
       }
     }

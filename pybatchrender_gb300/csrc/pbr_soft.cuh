@@ -53,7 +53,8 @@ __device__ __forceinline__ int soft_setup(const SceneParams& P, const SoftCtx& S
                                           float4 col, int inst_slot, bool smooth) {
   if (!(c0.z + c0.w >= 0.f && c1.z + c1.w >= 0.f && c2.z + c2.w >= 0.f)) return 0;
   SV s0 = to_screen(c0, S.W, S.H), s1 = to_screen(c1, S.W, S.H), s2 = to_screen(c2, S.W, S.H);
-  float area2 = (s1.x - s0.x) * (s2.y - s0.y) - (s2.x - s0.x) * (s1.y - s0.y);
+  // one explicit fused multiply-add, so that every kernel that inlines this rounds the same way
+  float area2 = fmaf(s1.x - s0.x, s2.y - s0.y, -((s2.x - s0.x) * (s1.y - s0.y)));
   if (!(area2 < 0.f)) return 0;  // back-facing, degenerate or NaN
   { SV t = s1; s1 = s2; s2 = t; }
   { float4 t = n1; n1 = n2; n2 = t; }

@@ -23,7 +23,9 @@ Reported variants (all on the same scene and states):
                through ``_step``'s torch copies + render captured in a CUDA
                graph; soft_fwd (differentiable soft-coverage forward, float32)
                and fwd_bwd (soft forward + adjoint kernel with a constant
-               dL/dout) on the same scene.
+               dL/dout) on the same scene; env_step_eager / env_step_graph:
+               the CartPole-v0 env step (dynamics, termination, reward,
+               auto-reset, pixels) from Python and replayed as one CUDA graph.
   roofline     the hard-raster kernel alone: algorithmic bytes per launch /
                mean CUDA-event duration, against the measured HBM copy peak.
   cpu_baseline the oracle's FP32 rasteriser (a CPU port of the reference's
@@ -317,6 +319,30 @@ def run_ours(args, world, rank, local):
         t = time_steps(soft_fwd_bwd, soft_steps, flush, stream)
         fwd_bwd_fps = N * soft_steps / (reduce_max(sum(t), world) / 1000.0)
 
+        # the CartPole env step (dynamics, termination, reward, auto-reset, pixels): eager, and replayed as
+        # one CUDA graph
+        import pybatchrender_gb300 as pbr
+        env = pbr.envs.make("CartPole-v0", num_scenes=N, tile_resolution=(res, res), device="cuda")
+        td0 = env.reset()
+        env_obs, env_sc = td0["observation"].clone(), td0["step_count"].clone()
+        env_acts = [torch.randint(0, 2, (N,), device=device) for _ in range(16)]
+
+        def env_eager(i):
+            env._step(pbr.env.TensorDict({"observation": env_obs, "action": env_acts[i % 16], "step_count": env_sc},
+                                         batch_size=[N]))
+        genv = pbr.GraphedEnvStep(env)
+
+        def env_graph(i):
+            genv({"observation": env_obs, "action": env_acts[i % 16], "step_count": env_sc})
+        env_steps = max(3, min(args.steps, 200))
+        for i in range(3):
+            env_eager(i)
+            env_graph(i)
+        t = time_steps(env_eager, env_steps, flush, stream)
+        env_eager_fps = N * env_steps / (reduce_max(sum(t), world) / 1000.0)
+        t = time_steps(env_graph, env_steps, flush, stream)
+        env_graph_fps = N * env_steps / (reduce_max(sum(t), world) / 1000.0)
+
         # end to end through the public API with host buffers: each step copies its states from pinned host
         # memory, renders into a fresh device tensor, and copies the pixels back to pinned host memory on a
         # second stream, so that step i's device-to-host copy overlaps step i+1's upload and render
@@ -366,7 +392,8 @@ def run_ours(args, world, rank, local):
                                        "bin_px": graph_r.cfg.bin_size}},
         "variants": {"batched_fused_step": value / world, "batched_graph_step_copies": copy_fps, "plain": plain_fps,
                      "graph_over_plain": (value / world) / plain_fps,
-                     "soft_fwd": soft_fwd_fps, "fwd_bwd": fwd_bwd_fps, "soft_fwd_over_fwd_bwd": soft_fwd_fps / fwd_bwd_fps},
+                     "soft_fwd": soft_fwd_fps, "fwd_bwd": fwd_bwd_fps, "soft_fwd_over_fwd_bwd": soft_fwd_fps / fwd_bwd_fps,
+                     "env_step_eager": env_eager_fps, "env_step_graph": env_graph_fps},
         "e2e": {"value": e2e_fps, "unit": UNIT, "h2d_bytes_per_step": int(N * 4 * 4),
                 "d2h_bytes_per_step": int(N * 3 * res * res)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

@@ -13,7 +13,7 @@ __version__ = "0.1.0"
 from .config import PBRConfig  # noqa: F401
 from .renderer import PBRCam, PBRLight, PBRNode, PBRRenderer, PBRShaderContext  # noqa: F401
 from ._capi import PBRError, RendererUnavailable  # noqa: F401
-from .env import PBREnv  # noqa: F401
+from .env import GraphedEnvStep, PBREnv  # noqa: F401
 from . import envs  # noqa: F401
 
 GPUFrameGrabber = None
@@ -26,7 +26,7 @@ except Exception:  # pragma: no cover
     GPU_AVAILABLE = False
 
 __all__ = [
-    "PBRConfig", "PBREnv", "PBRRenderer", "PBRNode", "PBRCam", "PBRLight", "PBRShaderContext",
+    "PBRConfig", "PBREnv", "GraphedEnvStep", "PBRRenderer", "PBRNode", "PBRCam", "PBRLight", "PBRShaderContext",
     "GPUFrameGrabber", "CPUFrameGrabber", "FrameGrabber", "envs", "__version__", "PBRError",
     "RendererUnavailable",
 ]

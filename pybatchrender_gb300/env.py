@@ -206,3 +206,61 @@ class PBREnv(_Base):
             pass
         renderer = renderer_cls(cfg)
         return env_cls(renderer=renderer, cfg=cfg)
+
+
+class GraphedEnvStep:
+    """``env._step`` replayed as one CUDA graph: the env's device-side
+    dynamics, termination, reward, auto-reset and the render launch it makes
+    (for CartPole a single state-bound raster launch) are captured on the
+    first call and replayed afterwards, so a step costs one graph launch
+    instead of a few dozen kernel launches from Python.
+
+    ``step(tensordict)`` takes ``observation``, ``action`` and optionally
+    ``step_count`` and returns the next tensordict of ``_step``.  Its tensors
+    are the graph's static outputs: they are overwritten by the next call, so
+    copy what must outlive it.  The graph is captured again when the input
+    shapes or dtypes change.  Random numbers (auto-reset states) come from
+    the CUDA generator through PyTorch's graph-safe RNG."""
+
+    def __init__(self, env: PBREnv, warmup: int = 2):
+        self.env = env
+        self.warmup = int(warmup)
+        self._graph = None
+        self._sig = None
+        self._static_in: dict = {}
+        self._static_out = None
+
+    def _inputs(self, tensordict) -> dict:
+        obs = tensordict["observation"]
+        ins = {"observation": obs, "action": tensordict["action"]}
+        sc = tensordict.get("step_count", None)
+        ins["step_count"] = sc if sc is not None else torch.zeros(obs.shape[:-1], dtype=torch.long, device=obs.device)
+        return {k: v.to(self.env.device) for k, v in ins.items()}
+
+    def _capture(self, ins: dict) -> None:
+        self._static_in = {k: v.detach().clone() for k, v in ins.items()}
+        td = TensorDict(dict(self._static_in), batch_size=self.env.batch_size)
+        side = torch.cuda.Stream(self.env.device)
+        side.wait_stream(torch.cuda.current_stream(self.env.device))
+        with torch.cuda.stream(side):
+            for _ in range(self.warmup):
+                self.env._step(td)
+        torch.cuda.current_stream(self.env.device).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._static_out = self.env._step(td)
+        self._graph = g
+
+    def step(self, tensordict):
+        ins = self._inputs(tensordict)
+        sig = tuple((k, tuple(v.shape), v.dtype) for k, v in sorted(ins.items()))
+        if self._graph is None or sig != self._sig:
+            self._capture(ins)
+            self._sig = sig
+        else:
+            for k, v in ins.items():
+                self._static_in[k].copy_(v, non_blocking=True)
+        self._graph.replay()
+        return self._static_out
+
+    __call__ = step

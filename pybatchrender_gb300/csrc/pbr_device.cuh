@@ -44,14 +44,9 @@ __device__ __forceinline__ void shade_rgb(const SceneParams& P, float nx, float 
   out[2] = col.z * ((1.f - s) + (P.amb[2] + ndl * P.lcol[2]) * s);
 }
 
-// Pose component c (0..2 position, 3..5 HPR) of buffer row `id`: from the
-// bound state matrix when the node has one for c, else from *own.
-__device__ __forceinline__ float bound_value(const NodeDesc& nd, long long id, int c, const float* own) {
-  if (nd.src && nd.src_col[c] >= 0) return nd.src[id * nd.src_stride + nd.src_col[c]];
-  return *own;
-}
-
-// Model matrix rows (3x4, row-major) of buffer row `id` of a node.
+// Model matrix rows (3x4, row-major) of buffer row `id` of a node.  All
+// loads are issued before any of them is used (the bound state's values
+// replace the node's own afterwards), so their latencies overlap.
 __device__ __forceinline__ void build_model(const NodeDesc& nd, long long id, float m[12]) {
   if (nd.mode == kModeMat) {
     const float* s = nd.rot + id * 16;
@@ -59,11 +54,21 @@ __device__ __forceinline__ void build_model(const NodeDesc& nd, long long id, fl
     for (int i = 0; i < 12; ++i) m[i] = s[i];
     return;
   }
+  const float* pp = nd.pos + id * 3;
+  float t[3] = {pp[0], pp[1], pp[2]};
+  const float s = nd.scale[id];
   float R[9];
   if (nd.mode == kModeHpr) {
-    float a[3];
+    const float* rp = nd.rot + id * 3;
+    float a[3] = {rp[0], rp[1], rp[2]};
+    if (nd.src) {
+      const float* sp = nd.src + id * nd.src_stride;
 #pragma unroll
-    for (int c = 0; c < 3; ++c) a[c] = bound_value(nd, id, 3 + c, nd.rot + id * 3 + c);
+      for (int c = 0; c < 3; ++c) {
+        if (nd.src_col[c] >= 0) t[c] = sp[nd.src_col[c]];
+        if (nd.src_col[3 + c] >= 0) a[c] = sp[nd.src_col[3 + c]];
+      }
+    }
     float sh, ch, sp, cp, sr, cr;
     sincosf(a[0], &sh, &ch);
     sincosf(a[1], &sp, &cp);
@@ -76,14 +81,19 @@ __device__ __forceinline__ void build_model(const NodeDesc& nd, long long id, fl
     const float* a = nd.rot + id * 9;
 #pragma unroll
     for (int i = 0; i < 9; ++i) R[i] = a[i];
+    if (nd.src) {
+      const float* sp = nd.src + id * nd.src_stride;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        if (nd.src_col[c] >= 0) t[c] = sp[nd.src_col[c]];
+    }
   }
-  const float s = nd.scale[id];
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     m[r * 4 + 0] = R[r * 3 + 0] * s;
     m[r * 4 + 1] = R[r * 3 + 1] * s;
     m[r * 4 + 2] = R[r * 3 + 2] * s;
-    m[r * 4 + 3] = bound_value(nd, id, r, nd.pos + id * 3 + r);
+    m[r * 4 + 3] = t[r];
   }
 }
 

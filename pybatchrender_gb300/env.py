@@ -72,12 +72,15 @@ def TensorDict(fields, batch_size=None):  # noqa: N802 - mirrors the tensordict 
 
 
 class _SpecLite:
-    def __init__(self, shape, dtype, device, n=None):
+    def __init__(self, shape, dtype, device, n=None, low=None, high=None):
         self.shape, self.dtype, self.device, self.n = torch.Size(shape), dtype, device, n
+        self.low, self.high = low, high
 
     def rand(self):
         if self.n is not None:
             return torch.randint(0, self.n, self.shape, dtype=self.dtype, device=self.device)
+        if self.low is not None:
+            return torch.empty(self.shape, dtype=self.dtype, device=self.device).uniform_(self.low, self.high)
         return torch.randn(self.shape, dtype=self.dtype, device=self.device)
 
     def zero(self):
@@ -123,8 +126,11 @@ class PBREnv(_Base):
 
     def set_default_specs(self, *, direct_obs_dim: int | None = None, actions: int | None = None,
                           with_pixels: bool = False, pixels_only: bool = False,
-                          discrete_actions: bool = True) -> None:
-        """Observation / action / reward / done specs (``env.py:33-82``)."""
+                          discrete_actions: bool = True, action_low: float | None = None,
+                          action_high: float | None = None) -> None:
+        """Observation / action / reward / done specs (``env.py:33-82``);
+        continuous actions are bounded when ``action_low`` / ``action_high``
+        are given (``envs/steering/env.py:142-156``)."""
         assert with_pixels or not pixels_only, "Cannot set both with_pixels and pixels_only to True."
         bs = self.batch_size if self.batch_size != torch.Size([]) else torch.Size([1])
         C = int(self.cfg.num_channels)
@@ -143,6 +149,11 @@ class PBREnv(_Base):
             self.observation_spec = Composite(**fields, shape=bs)
             if discrete_actions:
                 self.action_spec = Categorical(n=int(actions), shape=bs, dtype=torch.long, device=self.device)
+            elif action_low is not None:
+                from torchrl.data.tensor_specs import Bounded
+                self.action_spec = Bounded(low=float(action_low), high=float(action_high),
+                                           shape=bs + torch.Size([int(actions)]), dtype=torch.float32,
+                                           device=self.device)
             else:
                 self.action_spec = Unbounded(shape=bs + torch.Size([int(actions)]), dtype=torch.float32,
                                              device=self.device)
@@ -158,7 +169,9 @@ class PBREnv(_Base):
         if discrete_actions:
             self.action_spec = _SpecLite(bs, torch.long, self.device, n=int(actions))
         else:
-            self.action_spec = _SpecLite(bs + torch.Size([int(actions)]), torch.float32, self.device)
+            self.action_spec = _SpecLite(bs + torch.Size([int(actions)]), torch.float32, self.device,
+                                         low=None if action_low is None else float(action_low),
+                                         high=None if action_high is None else float(action_high))
         self.reward_spec = _SpecLite(bs + torch.Size([1]), torch.float32, self.device)
         self.done_spec = _SpecLite(bs + torch.Size([1]), torch.bool, self.device)
 

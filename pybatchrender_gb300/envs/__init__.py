@@ -64,6 +64,8 @@ def make_parallel(name: str, num_workers: int, shared_memory: bool = True, **con
 def _register_builtins() -> None:
     from .cartpole import CartPoleConfig, CartPoleEnv, CartPoleRenderer
     register("CartPole-v0", CartPoleEnv, CartPoleRenderer, CartPoleConfig)
+    from .steering import SteeringConfig, SteeringEnv, SteeringRenderer
+    register("Steering-v0", SteeringEnv, SteeringRenderer, SteeringConfig)
 
 
 def _register_from_entry_points() -> None:

@@ -270,6 +270,8 @@ _BUILTIN = {
     "cylinder": lambda: cylinder(64),
     "sphere": lambda: icosphere(2),
     "icosphere": lambda: icosphere(2),
+    # Panda3D's bundled smiley (a textured sphere) is not available: an untextured sphere stands in
+    "smiley": lambda: icosphere(2),
 }
 
 

@@ -94,6 +94,12 @@ class PBRNode(PBRShaderContext):
         self.counts = None  # [N] int32 active instances per scene (uneven batching)
         self._register_self()
 
+    def remove(self) -> None:
+        """Remove this node from its renderer (``NodePath.removeNode``)."""
+        remove = getattr(self.base, "remove_node", None)
+        if remove is not None:
+            remove(self)
+
     # ------------------------------------------------------------------ state
     def _as(self, x, cols: int | None) -> torch.Tensor:
         t = torch.as_tensor(x, dtype=torch.float32)

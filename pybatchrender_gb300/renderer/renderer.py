@@ -98,6 +98,17 @@ class PBRRenderer:
             self._build_context()
         return node
 
+    def remove_node(self, node: PBRNode) -> None:
+        """Remove a node from the scene (Panda3D's ``NodePath.removeNode`` in
+        the reference, e.g. ``envs/steering/renderer.py:171-179`` when the
+        obstacles are rebuilt).  Its state bindings go with it."""
+        if node in self._pbr_nodes:
+            self._pbr_nodes.remove(node)
+        self._state_bindings = [b for b in self._state_bindings if b[0] is not node]
+        self._graph = None
+        if self._ctx is not None:
+            self._build_context()
+
     def add_camera(self, fov_y_deg: float = 55.0, z_near: float = 0.05, z_far: float = 100.0,
                    fixed_projection: bool = True) -> PBRCam:
         self._pbr_cam = PBRCam(self, num_scenes=self.cfg.num_scenes, cols=self.cfg.tiles[0], rows=self.cfg.tiles[1],

@@ -105,7 +105,8 @@ def test_meshes_and_baking():
     with pytest.raises(ValueError):
         meshes.bake(box, (1.0, 2.0), None, None)
     with pytest.raises(FileNotFoundError):
-        meshes.resolve_model("models/smiley")
+        meshes.resolve_model("models/teapot")
+    assert meshes.resolve_model("models/smiley").num_triangles == 320  # untextured sphere stand-in
 
 
 def test_env_without_renderer_pixels():
@@ -150,3 +151,37 @@ def test_bind_state_validation():
         r.bind_state(r.cart, "x", -1)
     # no CUDA context: the fused path is never taken
     assert r._bound_state((torch.zeros(4, 4),), {}) is None
+
+
+def test_steering_env_dynamics_cpu():
+    """Steering-v0 without pixels: obstacle layout, forward motion, passages
+    speed the player up, a collision outside the grace period is penalised."""
+    env = envs.make("Steering-v0", num_scenes=4, device="cpu", render=False, number_of_obstacles=5,
+                    distance_to_first_obstacle=2.0, obstacle_y_spacing=3.0)
+    td = env.reset()
+    obs = td["observation"]
+    assert obs.shape == (4, 6)
+    ob = env._obstacles
+    assert ob.shape == (4, 5, 4)
+    assert torch.allclose(ob[0, :, 1], torch.tensor([2.0, 5.0, 8.0, 11.0, 14.0]))
+    assert set(ob[:, :, 0].unique().tolist()) <= set(float(v) for v in range(-11, 12, 2))
+    # put every player on the first obstacle's lane: the first passage is a hit
+    env._player_x = ob[:, 0, 0].clone()
+    td = pbr.env.TensorDict({"observation": env._get_observation(), "action": torch.zeros(4, 1),
+                             "step_count": torch.zeros(4, dtype=torch.long)}, batch_size=[4])
+    y0 = env._player_y.clone()
+    nxt = env._step(td)
+    assert torch.allclose(env._player_y, y0 + 96.0 / 60.0)  # speed_initial * tau, one step
+    assert (nxt["reward"] == 0.0).all()  # y = 1.6: the first obstacle (y = 2) is not passed yet
+    nxt = env._step(pbr.env.TensorDict({"observation": nxt["observation"], "action": torch.zeros(4, 1),
+                                        "step_count": nxt["step_count"]}, batch_size=[4]))
+    assert (nxt["reward"] == -1.0).all() and (nxt["observation"][:, 3] == 1.0).all()  # hit, grace active
+    assert torch.allclose(env._forward_speed, torch.full((4,), 96.0 + 0.072 - 6.12))
+    # a second hit inside the grace period is not penalised
+    env._player_x = ob[:, 1, 0].clone()
+    for _ in range(2):
+        nxt = env._step(pbr.env.TensorDict({"observation": nxt["observation"], "action": torch.zeros(4, 1),
+                                            "step_count": nxt["step_count"]}, batch_size=[4]))
+    assert (nxt["reward"] == 0.0).all()
+    a = env.action_spec.rand()
+    assert a.shape == (4, 1) and (a.abs() <= 327.68).all()

@@ -73,6 +73,13 @@ int pbr_destroy(pbr_ctx* ctx);
 int pbr_mesh_register(pbr_ctx* ctx, const float* d_pos, const float* d_nrm, const int32_t* d_idx,
                       int nv, int nt, int smooth, int* out_mesh_id);
 
+/* Attach texture coordinates to a registered mesh: d_uv [nv,2] float32
+ * (GL convention, v = 0 at the bottom of the image), or NULL for none (all
+ * coordinates 0).  Replaces the p3d_MultiTexCoord0 vertex column that
+ * Panda3D's model loader provides (renderer/node.py:61-71,
+ * shaders/basic.vert:16,56). */
+int pbr_mesh_set_uv(pbr_ctx* ctx, int mesh_id, const float* d_uv);
+
 /* Add a node: one mesh drawn instances_per_scene times in every scene.
  * shared != 0 means instance i of every scene reads buffer row i
  * (B = instances_per_scene rows), otherwise scene k instance i reads row
@@ -89,6 +96,17 @@ int pbr_node_add(pbr_ctx* ctx, int mesh_id, int instances_per_scene, int shared,
  * (renderer/node.py:110-178): the kernels build M = [R*s | t] themselves. */
 int pbr_node_set_buffers(pbr_ctx* ctx, int node_id, int mode, const float* d_pos, const float* d_rot,
                          const float* d_scale, const float* d_color, const int32_t* d_counts);
+
+/* Texture a node (useTexture = 1): d_rgba [height,width,4] uint8 RGBA on the
+ * device, row 0 at v = 0 (the bottom row of the image, Panda3D's image
+ * origin), 4-byte aligned; NULL removes the texture (useTexture = 0).
+ * Sampled per pixel with bilinear filtering and repeat wrap at the
+ * perspective-correct texture coordinates; the shaded colour becomes
+ * texel.rgb * colour.rgb * light.  Hard raster only: the soft-mode calls
+ * fail with PBR_ERR_INVALID while a node is textured.  Replaces
+ * PBRNode.set_texture (renderer/node.py:277-287) and the p3d_Texture0 sample
+ * of shaders/basic.frag:31-32. */
+int pbr_node_set_texture(pbr_ctx* ctx, int node_id, const uint8_t* d_rgba, int width, int height);
 
 /* Bind pose component `component` of a node to column `column` of a per-step
  * state matrix: 0..2 = position x, y, z; 3..5 = heading, pitch, roll (HPR

@@ -17,7 +17,8 @@ Scene format (the same fp32 arrays the CUDA kernels read; produced by
 * ``nodes``: list of dicts with ``mesh`` (index), ``I`` (instances per scene),
   ``shared``, ``mode`` (0 = HPR, 1 = 3x3 rotation, 2 = 4x4 matrix), ``counts``
   (``[N]`` int32 or None), ``pos [B,3]``, ``rot`` (``[B,3]`` / ``[B,9]`` / ``[B,16]``),
-  ``scale [B]``, ``color [B,4]``.
+  ``scale [B]``, ``color [B,4]``, optional ``texture`` ``[h,w,4]`` uint8 RGBA (row 0
+  at v = 0, i.e. the bottom row of the image) sampled at the mesh's ``uvs [nv,2]``.
 """
 from __future__ import annotations
 
@@ -35,14 +36,16 @@ MODE_HPR, MODE_ROT, MODE_MAT = 0, 1, 2
 
 class OrcMesh(ctypes.Structure):
     _fields_ = [("nv", ctypes.c_int32), ("nt", ctypes.c_int32),
-                ("pos", ctypes.c_void_p), ("nrm", ctypes.c_void_p), ("idx", ctypes.c_void_p)]
+                ("pos", ctypes.c_void_p), ("nrm", ctypes.c_void_p), ("idx", ctypes.c_void_p),
+                ("uv", ctypes.c_void_p)]
 
 
 class OrcNode(ctypes.Structure):
     _fields_ = [("mesh", ctypes.c_int32), ("inst_per_scene", ctypes.c_int32),
                 ("shared", ctypes.c_int32), ("mode", ctypes.c_int32),
                 ("counts", ctypes.c_void_p), ("pos", ctypes.c_void_p), ("rot", ctypes.c_void_p),
-                ("scale", ctypes.c_void_p), ("color", ctypes.c_void_p)]
+                ("scale", ctypes.c_void_p), ("color", ctypes.c_void_p),
+                ("tex", ctypes.c_void_p), ("tex_w", ctypes.c_int32), ("tex_h", ctypes.c_int32)]
 
 
 class OrcScene(ctypes.Structure):
@@ -129,9 +132,11 @@ class _Packed:
         for i, m in enumerate(meshes):
             pos, nrm, idx = (m["positions"], m["normals"], m["indices"]) if isinstance(m, dict) else \
                 (m.positions, m.normals, m.indices)
+            uv = m.get("uvs") if isinstance(m, dict) else getattr(m, "uvs", None)
             p, n, ix = f32(pos, (-1, 3)), f32(nrm, (-1, 3)), i32(np.asarray(idx).reshape(-1, 3))
             self.meshes[i].nv, self.meshes[i].nt = p.shape[0], ix.shape[0]
             self.meshes[i].pos, self.meshes[i].nrm, self.meshes[i].idx = _ptr(p), _ptr(n), _ptr(ix)
+            self.meshes[i].uv = _ptr(f32(uv, (-1, 2))) if uv is not None else None
         self.nodes = (OrcNode * max(1, len(nodes)))()
         for i, nd in enumerate(nodes):
             o = self.nodes[i]
@@ -142,6 +147,13 @@ class _Packed:
             o.rot = _ptr(f32(nd["rot"]).reshape(-1))
             o.scale = _ptr(f32(nd["scale"]).reshape(-1))
             o.color = _ptr(f32(nd["color"], (-1, 4)))
+            tex = nd.get("texture")
+            if tex is not None:
+                t = np.ascontiguousarray(np.asarray(tex, dtype=np.uint8))
+                if t.ndim != 3 or t.shape[2] != 4:
+                    raise ValueError("node texture must be [h, w, 4] uint8")
+                self.keep.append(t)
+                o.tex, o.tex_h, o.tex_w = _ptr(t), t.shape[0], t.shape[1]
         self.nmeshes, self.nnodes = len(meshes), len(nodes)
 
 

@@ -14,10 +14,12 @@
  *   shaders/basic.vert:24-57     instance decode (scene = gid / I, inst = gid % I,
  *                                id = shared ? inst : gid), clip = VP[scene] * M[id] * v,
  *                                v_normal = normalize(mat3(M) * n), v_color = colbuf[id]
- *   shaders/basic.frag:20-39     tile discard, base = 1 (useTexture = 0),
+ *   shaders/basic.frag:20-39     tile discard, base = 1 (useTexture = 0) or the
+ *                                bilinear texture sample at the perspective-correct
+ *                                v_uv (useTexture = 1: renderer/node.py:277-287),
  *                                ndl = max(dot(normalize(n), normalize(L)), 0),
  *                                l = mix(1, ambient + ndl * col, clamp(strength, 0, 1)),
- *                                rgb = color.rgb * l, a = color.a
+ *                                rgb = base * color.rgb * l, a = color.a
  *   renderer/shader_context.py:47-84  R = Rz(H) Ry(P) Rx(R), M = [R*s | t]
  *   renderer/node.py:116-126     M[:3,:3] = rot3 * scale, M[:3,3] = position
  *   renderer/camera.py:110-135 + shaders/basic.vert:45-52
@@ -36,6 +38,10 @@
  * clear, equal depths resolved by draw order (node, then instance, then
  * triangle), window depth = 0.5 * z_ndc + 0.5, screen-linear depth and
  * perspective-correct normal interpolation, UNORM8 = floor(clamp(c,0,1)*255+0.5).
+ * Textures follow GL's sampler defaults that Panda3D applies to a loaded
+ * texture (linear min/mag filter without mipmaps, repeat wrap): texel
+ * centres at (i + 0.5) / w, texel row 0 at v = 0 (the bottom row of the
+ * image, Panda3D's image origin), RGBA8 texels read as c / 255.
  */
 #include <math.h>
 #include <tgmath.h> /* sin/cos/sqrt/exp follow REAL: float math in the FP32 build */
@@ -68,6 +74,7 @@ typedef struct {
     const float* pos;    /* [nv*3] */
     const float* nrm;    /* [nv*3] */
     const int32_t* idx;  /* [nt*3] */
+    const float* uv;     /* [nv*2] texture coordinates, or NULL (all 0) */
 } orc_mesh;
 
 typedef struct {
@@ -80,6 +87,8 @@ typedef struct {
     const float* rot;       /* HPR [B*3] radians | ROT [B*9] | MAT [B*16] row-major */
     const float* scale;     /* [B] (ignored for MAT) */
     const float* color;     /* [B*4] */
+    const uint8_t* tex;     /* [tex_h][tex_w][4] RGBA8, row 0 at v = 0; NULL: untextured */
+    int32_t tex_w, tex_h;
 } orc_node;
 
 typedef struct {
@@ -132,9 +141,13 @@ static void build_instance(const orc_node* nd, int64_t id, inst_xf* out) {
 typedef struct {
     real x, y, z, w;        /* clip coordinates */
     real n[3];              /* world normal (normalised, basic.vert:53) */
+    real u, v;              /* texture coordinates (basic.vert:56) */
 } cvert;
 
-static void xform_vertex(const inst_xf* xf, const real* VP, const float* p, const float* n, cvert* o) {
+static void xform_vertex(const inst_xf* xf, const real* VP, const float* p, const float* n, const float* uv,
+                         cvert* o) {
+    o->u = uv ? (real)uv[0] : 0;
+    o->v = uv ? (real)uv[1] : 0;
     real wx = xf->m[0] * p[0] + xf->m[1] * p[1] + xf->m[2] * p[2] + xf->m[3];
     real wy = xf->m[4] * p[0] + xf->m[5] * p[1] + xf->m[6] * p[2] + xf->m[7];
     real wz = xf->m[8] * p[0] + xf->m[9] * p[1] + xf->m[10] * p[2] + xf->m[11];
@@ -167,6 +180,8 @@ static int clip_near(const cvert* in, cvert* out) {
             v.z = a->z + t * (b->z - a->z);
             v.w = a->w + t * (b->w - a->w);
             for (int k = 0; k < 3; ++k) v.n[k] = a->n[k] + t * (b->n[k] - a->n[k]);
+            v.u = a->u + t * (b->u - a->u);
+            v.v = a->v + t * (b->v - a->v);
             out[n++] = v;
         }
     }
@@ -176,6 +191,8 @@ static int clip_near(const cvert* in, cvert* out) {
 typedef struct {
     real sx[3], sy[3], sz[3], iw[3];   /* screen x, y (pixels, y down), window depth, 1/w */
     real n[3][3];
+    real uv[3][2];
+    const orc_node* tex_node;          /* node whose texture is sampled, or NULL */
     real A[3], B[3], Cc[3];            /* edge functions, edge k opposite vertex k */
     int tl[3];
     real area2;
@@ -207,7 +224,10 @@ static int setup_tri(const orc_scene* sc, const cvert* v0, const cvert* v1, cons
         t->sz[k] = v[k]->z * iw * (real)0.5 + (real)0.5;
         t->iw[k] = iw;
         for (int c = 0; c < 3; ++c) t->n[k][c] = v[k]->n[c];
+        t->uv[k][0] = v[k]->u;
+        t->uv[k][1] = v[k]->v;
     }
+    t->tex_node = NULL;
     real area2 = (t->sx[1] - t->sx[0]) * (t->sy[2] - t->sy[0]) - (t->sx[2] - t->sx[0]) * (t->sy[1] - t->sy[0]);
     /* GL front faces are counter-clockwise with y up, i.e. area2 < 0 with y down */
     if (area2 == 0) return 0;
@@ -220,6 +240,7 @@ static int setup_tri(const orc_scene* sc, const cvert* v0, const cvert* v1, cons
 #define SWP(a, b) (tmp = (a), (a) = (b), (b) = tmp)
         SWP(t->sx[1], t->sx[2]); SWP(t->sy[1], t->sy[2]); SWP(t->sz[1], t->sz[2]); SWP(t->iw[1], t->iw[2]);
         for (int c = 0; c < 3; ++c) SWP(t->n[1][c], t->n[2][c]);
+        SWP(t->uv[1][0], t->uv[2][0]); SWP(t->uv[1][1], t->uv[2][1]);
 #undef SWP
         area2 = -area2;
     }
@@ -273,6 +294,28 @@ static void shade(const orc_scene* sc, const real Ln[3], const real n_in[3], con
     out[3] = col[3];
 }
 
+/* GL bilinear sample with repeat wrap of an RGBA8 texture (row 0 at v = 0). */
+static void sample_texture(const orc_node* nd, real u, real v, real out[3]) {
+    const int w = nd->tex_w, h = nd->tex_h;
+    real fu = u - floor(u), fv = v - floor(v);
+    real x = fu * w - (real)0.5, y = fv * h - (real)0.5;
+    real fx = floor(x), fy = floor(y);
+    real ax = x - fx, ay = y - fy;
+    /* fx lies in [-1, w - 1]; -1 wraps to w - 1 (so does a NaN coordinate) */
+    int x0 = (fx >= 0 && fx <= w - 1) ? (int)fx : w - 1;
+    int y0 = (fy >= 0 && fy <= h - 1) ? (int)fy : h - 1;
+    int x1 = x0 + 1 == w ? 0 : x0 + 1, y1 = y0 + 1 == h ? 0 : y0 + 1;
+    const uint8_t* t00 = nd->tex + ((int64_t)y0 * w + x0) * 4;
+    const uint8_t* t10 = nd->tex + ((int64_t)y0 * w + x1) * 4;
+    const uint8_t* t01 = nd->tex + ((int64_t)y1 * w + x0) * 4;
+    const uint8_t* t11 = nd->tex + ((int64_t)y1 * w + x1) * 4;
+    for (int c = 0; c < 3; ++c) {
+        real top = (1 - ax) * (t00[c] / (real)255) + ax * (t10[c] / (real)255);
+        real bot = (1 - ax) * (t01[c] / (real)255) + ax * (t11[c] / (real)255);
+        out[c] = (1 - ay) * top + ay * bot;
+    }
+}
+
 static void light_dir(const orc_scene* sc, real Ln[3]) {
     real lx = sc->ldir[0], ly = sc->ldir[1], lz = sc->ldir[2];
     real ln = sqrt(lx * lx + ly * ly + lz * lz);
@@ -315,7 +358,7 @@ static void walk_scene(const orc_scene* sc, int nmeshes, const orc_mesh* meshes,
             inst_xf xf;
             build_instance(nd, id, &xf);
             for (int v = 0; v < me->nv; ++v)
-                xform_vertex(&xf, VP, me->pos + 3 * v, me->nrm + 3 * v, &cache[v]);
+                xform_vertex(&xf, VP, me->pos + 3 * v, me->nrm + 3 * v, me->uv ? me->uv + 2 * v : NULL, &cache[v]);
             int32_t wid_base = (int32_t)((rank_base + i) * max_tris);
             for (int t = 0; t < me->nt; ++t) {
                 cvert tv[3];
@@ -334,6 +377,7 @@ static void walk_scene(const orc_scene* sc, int nmeshes, const orc_mesh* meshes,
                     stri st;
                     real margin = soft ? (real)SOFT_CUTOFF * (real)sc->sigma + 1 : 0;
                     if (!setup_tri(sc, &poly[0], &poly[f], &poly[f + 1], &st, margin)) continue;
+                    st.tex_node = nd->tex ? nd : NULL;
                     cb(user, &st, xf.c, wid_base + t);
                 }
             }
@@ -378,7 +422,18 @@ static void hard_pass1(void* user, const stri* t, const real col[4], int32_t wid
             real qs = q0 + q1 + q2;
             real nn[3];
             for (int c = 0; c < 3; ++c) nn[c] = (q0 * t->n[0][c] + q1 * t->n[1][c] + q2 * t->n[2][c]) / qs;
-            shade(sc, h->Ln, nn, col, &h->rgba[o * 4]);
+            if (t->tex_node) {
+                /* basic.frag:31-32,38: base * v_color.rgb */
+                real u = (q0 * t->uv[0][0] + q1 * t->uv[1][0] + q2 * t->uv[2][0]) / qs;
+                real v = (q0 * t->uv[0][1] + q1 * t->uv[1][1] + q2 * t->uv[2][1]) / qs;
+                real base[3], tc[4];
+                sample_texture(t->tex_node, u, v, base);
+                for (int c = 0; c < 3; ++c) tc[c] = base[c] * col[c];
+                tc[3] = col[3];
+                shade(sc, h->Ln, nn, tc, &h->rgba[o * 4]);
+            } else {
+                shade(sc, h->Ln, nn, col, &h->rgba[o * 4]);
+            }
         }
     }
 }

@@ -34,7 +34,9 @@ SIGNATURES: dict[str, list] = {
     "pbr_create": [ctypes.POINTER(_vp), _i, _i, _i, _i, _i],
     "pbr_destroy": [_vp],
     "pbr_mesh_register": [_vp, _vp, _vp, _vp, _i, _i, _i, _pi],
+    "pbr_mesh_set_uv": [_vp, _i, _vp],
     "pbr_node_add": [_vp, _i, _i, _i, _pi],
+    "pbr_node_set_texture": [_vp, _i, _vp, _i, _i],
     "pbr_node_set_buffers": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp],
     "pbr_camera_bind": [_vp, _vp, _f, _f],
     "pbr_light_set": [_vp, _f3, _f3, _f3, _f],

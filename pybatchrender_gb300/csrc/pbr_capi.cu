@@ -41,7 +41,7 @@ struct pbr_ctx {
   float* d_zbuf = nullptr;
   uint32_t* d_cbuf = nullptr;
   // cudaFuncSetAttribute cache: [threads idx][plain][winner]
-  int smem_set[3][2][2] = {};
+  int smem_set[3][2][2][2] = {};
   int small_smem_set[2][2][2] = {};
   int soft_small_smem_set[2] = {};
   int soft_large_smem_set[2] = {};
@@ -139,6 +139,7 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
     max_nv = std::max(max_nv, me.nv);
     max_inst_verts = std::max(max_inst_verts, (long long)nd.ips * me.nv);
     if (me.smooth) A.smooth_any = 1;
+    if (nd.tex) A.smooth_any = A.tex_any = 1;  // textured triangles are shaded per pixel
   }
   // no vertex cache: each thread transforms its own triangle's vertices
   A.vcap = 0;
@@ -174,15 +175,15 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
                    "reduce mesh size or threads", L.total, ctx->max_smem);
   }
   // kernel attribute + occupancy
-  int& cached = ctx->smem_set[threads_index(threads)][plain ? 1 : 0][winner ? 1 : 0];
+  int& cached = ctx->smem_set[threads_index(threads)][plain ? 1 : 0][winner ? 1 : 0][A.tex_any ? 1 : 0];
   if (out->smem > 48 * 1024 && out->smem > cached) {
-    cudaError_t e = pbr::hard_set_smem_limit(threads, plain, winner, out->smem);
+    cudaError_t e = pbr::hard_set_smem_limit(threads, plain, winner, A.tex_any != 0, out->smem);
     if (e != cudaSuccess) return cuda_err(ctx, e, "cudaFuncSetAttribute");
     cached = out->smem;
   }
   if (persistent) {
     int bps = 0;
-    cudaError_t e = pbr::hard_occupancy(threads, plain, winner, out->smem, &bps);
+    cudaError_t e = pbr::hard_occupancy(threads, plain, winner, A.tex_any != 0, out->smem, &bps);
     if (e != cudaSuccess) return cuda_err(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     out->grid = std::max(1, std::min(A.num_items, ctx->sm_count * std::max(1, bps)));
   } else {
@@ -213,6 +214,7 @@ static int plan_small(pbr_ctx* ctx, bool plain, bool winner, int n0, int n1, Lau
     insts += nd.ips;
     verts += (long long)nd.ips * me.nv;
     if (me.smooth) A.smooth_any = 1;
+    if (nd.tex) return set_err(ctx, PBR_ERR_CAPACITY, "textured nodes are drawn by the tile kernel");
   }
   if (insts > 32 || verts > 256)
     return set_err(ctx, PBR_ERR_CAPACITY, "scene too large for the scene-per-warp kernel");
@@ -357,6 +359,32 @@ int pbr_mesh_register(pbr_ctx* ctx, const float* d_pos, const float* d_nrm, cons
   m.smooth = smooth ? 1 : 0;
   ctx->P.max_tris = std::max(ctx->P.max_tris, nt);
   *out_mesh_id = ctx->P.num_meshes++;
+  return PBR_OK;
+}
+
+int pbr_mesh_set_uv(pbr_ctx* ctx, int mesh_id, const float* d_uv) {
+  PBR_CHECK_CTX(ctx);
+  if (mesh_id < 0 || mesh_id >= ctx->P.num_meshes) return set_err(ctx, PBR_ERR_INVALID, "unknown mesh id %d", mesh_id);
+  if (((uintptr_t)d_uv & 7u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_uv must be 8-byte aligned");
+  ctx->P.meshes[mesh_id].uv = d_uv;
+  return PBR_OK;
+}
+
+int pbr_node_set_texture(pbr_ctx* ctx, int node_id, const uint8_t* d_rgba, int width, int height) {
+  PBR_CHECK_CTX(ctx);
+  if (node_id < 0 || node_id >= ctx->P.num_nodes) return set_err(ctx, PBR_ERR_INVALID, "unknown node id %d", node_id);
+  NodeDesc& nd = ctx->P.nodes[node_id];
+  if (!d_rgba) {
+    nd.tex = nullptr;
+    nd.tex_w = nd.tex_h = 0;
+    return PBR_OK;
+  }
+  if (width <= 0 || height <= 0 || width > 16384 || height > 16384)
+    return set_err(ctx, PBR_ERR_INVALID, "texture size must be 1..16384 in each dimension (got %d x %d)", width, height);
+  if (((uintptr_t)d_rgba & 3u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_rgba must be 4-byte aligned");
+  nd.tex = reinterpret_cast<const uint32_t*>(d_rgba);
+  nd.tex_w = width;
+  nd.tex_h = height;
   return PBR_OK;
 }
 
@@ -864,9 +892,17 @@ int pbr_node_set_grads(pbr_ctx* ctx, int node_id, float* d_gpos, float* d_ghpr, 
   return PBR_OK;
 }
 
+static int reject_textures(pbr_ctx* ctx) {
+  for (int n = 0; n < ctx->P.num_nodes; ++n)
+    if (ctx->P.nodes[n].tex)
+      return set_err(ctx, PBR_ERR_INVALID, "node %d is textured: the soft mode draws untextured nodes only", n);
+  return PBR_OK;
+}
+
 int pbr_render_soft(pbr_ctx* ctx, float* d_out, float* d_stats, void* stream) {
   PBR_CHECK_CTX(ctx);
   if (!d_out) return set_err(ctx, PBR_ERR_INVALID, "d_out is null");
+  if (reject_textures(ctx)) return PBR_ERR_INVALID;
   if (((uintptr_t)d_stats & 15u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_stats must be 16-byte aligned");
   int rc = check_ready(ctx, 0, ctx->P.num_nodes);
   if (rc) return rc;
@@ -893,6 +929,7 @@ int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, co
                       float* d_grad_light, void* stream) {
   PBR_CHECK_CTX(ctx);
   if (!d_out || !d_stats || !d_grad_out) return set_err(ctx, PBR_ERR_INVALID, "d_out, d_stats and d_grad_out are required");
+  if (reject_textures(ctx)) return PBR_ERR_INVALID;
   if (((uintptr_t)d_stats & 15u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_stats must be 16-byte aligned");
   int rc = check_ready(ctx, 0, ctx->P.num_nodes);
   if (rc) return rc;

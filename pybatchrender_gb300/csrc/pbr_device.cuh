@@ -134,6 +134,8 @@ struct SetupCtx {
   float4* S1;
   float4* S2;
   float4* S3;
+  float4* S4;
+  float4* S5;
   float W, H;
   float ry0, ry1;  // region rows (inclusive)
   int cull;
@@ -152,13 +154,25 @@ __device__ __forceinline__ float4 make_edge(float xa, float ya, float xb, float 
   return make_float4(A, B, xf, yf);
 }
 
+// Texture input of one triangle: its vertices' texture coordinates and the
+// node whose texture it samples (node < 0: untextured).
+struct TexIn {
+  float2 t0 = {0.f, 0.f}, t1 = {0.f, 0.f}, t2 = {0.f, 0.f};
+  int node = -1;
+};
+
+__device__ __forceinline__ float2 mesh_uv(const MeshDesc& me, int i) {
+  return me.uv ? make_float2(me.uv[2 * i], me.uv[2 * i + 1]) : make_float2(0.f, 0.f);
+}
+
 // Triangle setup from screen-space vertices (to_screen of the clip
 // coordinates).  Returns 1 when the triangle is kept (and, if WRITE, its
 // records are written at slot), 0 when it is culled or covers no pixel centre.
+// A textured triangle (tx.node >= 0) is shaded per pixel: pass smooth = true.
 template <bool WRITE>
 __device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx& S, SV v0, float4 n0, SV v1,
                                             float4 n1, SV v2, float4 n2, int slot, float4 col, int draw_id,
-                                            bool smooth) {
+                                            bool smooth, TexIn tx = TexIn()) {
   // one explicit fused multiply-add, so that every kernel that inlines this rounds the same way
   float area2 = fmaf(v1.x - v0.x, v2.y - v0.y, -((v2.x - v0.x) * (v1.y - v0.y)));
   if (S.cull) {
@@ -169,6 +183,7 @@ __device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx
   if (area2 < 0.f) {
     SV t = v1; v1 = v2; v2 = t;
     float4 tn = n1; n1 = n2; n2 = tn;
+    float2 tt = tx.t1; tx.t1 = tx.t2; tx.t2 = tt;
     area2 = -area2;
   }
   const float mnx = fminf(fminf(v0.x, v1.x), v2.x), mxx = fmaxf(fmaxf(v0.x, v1.x), v2.x);
@@ -189,7 +204,9 @@ __device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx
   const float zC = fmaf(-zB, v0.y, fmaf(-zA, v0.x, v0.z));
   const uint32_t xbox = (uint32_t)fx0 | ((uint32_t)fx1 << 16);
   const uint32_t ybox = (uint32_t)fy0 | ((uint32_t)fy1 << 16);
-  const uint32_t flags = (tl0 ? 1u : 0u) | (tl1 ? 2u : 0u) | (tl2 ? 4u : 0u) | (smooth ? 8u : 0u);
+  const bool textured = smooth && tx.node >= 0;
+  const uint32_t flags =
+      (tl0 ? 1u : 0u) | (tl1 ? 2u : 0u) | (tl2 ? 4u : 0u) | (smooth ? 8u : 0u) | (textured ? 16u : 0u);
   const uint32_t color = smooth ? 0u : shade_pack(P, n0.x, n0.y, n0.z, col);
   S.T0[slot] = e0;
   S.T1[slot] = e1;
@@ -202,6 +219,10 @@ __device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx
     S.S1[slot] = make_float4(n1.x, n1.y, n1.z, v1.iw);
     S.S2[slot] = make_float4(n2.x, n2.y, n2.z, v2.iw);
     S.S3[slot] = col;
+    if (textured) {
+      S.S4[slot] = make_float4(tx.t0.x, tx.t0.y, tx.t1.x, tx.t1.y);
+      S.S5[slot] = make_float4(tx.t2.x, tx.t2.y, __int_as_float(tx.node), 0.f);
+    }
   }
   return 1;
 }
@@ -209,13 +230,17 @@ __device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx
 template <bool WRITE>
 __device__ __forceinline__ int setup_tri(const SceneParams& P, const SetupCtx& S, float4 c0, float4 n0, float4 c1,
                                          float4 n1, float4 c2, float4 n2, int slot, float4 col, int draw_id,
-                                         bool smooth) {
+                                         bool smooth, const TexIn& tx) {
   const SV v0 = to_screen(c0, S.W, S.H), v1 = to_screen(c1, S.W, S.H), v2 = to_screen(c2, S.W, S.H);
-  return setup_tri_sv<WRITE>(P, S, v0, n0, v1, n1, v2, n2, slot, col, draw_id, smooth);
+  return setup_tri_sv<WRITE>(P, S, v0, n0, v1, n1, v2, n2, slot, col, draw_id, smooth, tx);
 }
 
 __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
   return make_float4(a.x + t * (b.x - a.x), a.y + t * (b.y - a.y), a.z + t * (b.z - a.z), a.w + t * (b.w - a.w));
+}
+
+__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float t) {
+  return make_float2(a.x + t * (b.x - a.x), a.y + t * (b.y - a.y));
 }
 
 // Near-plane clip (Sutherland-Hodgman against z + w >= 0: at most 4
@@ -226,29 +251,39 @@ __device__ __forceinline__ float4 lerp4(float4 a, float4 b, float t) {
 template <bool WRITE>
 __device__ __forceinline__ int clip_tri(const SceneParams& P, const SetupCtx& S, float4 c0, float4 n0, float4 c1,
                                      float4 n1, float4 c2, float4 n2, int i0, int i1, int i2, int slot, float4 col,
-                                     int draw_id, bool smooth) {
+                                     int draw_id, bool smooth, const TexIn& tx = TexIn()) {
   const float4 c[3] = {c0, c1, c2};
   const float4 n[3] = {n0, n1, n2};
+  const float2 uv[3] = {tx.t0, tx.t1, tx.t2};
   const int id[3] = {i0, i1, i2};
   const float d[3] = {c0.z + c0.w, c1.z + c1.w, c2.z + c2.w};
   float4 pc[4], pn[4];
+  float2 pt[4];
   int np = 0;
 #pragma unroll
   for (int e = 0; e < 3; ++e) {
     const int a = e, b = (e + 1) % 3;
     const bool ina = d[a] >= 0.f, inb = d[b] >= 0.f;
-    if (ina) { pc[np] = c[a]; pn[np] = n[a]; ++np; }
+    if (ina) { pc[np] = c[a]; pn[np] = n[a]; pt[np] = uv[a]; ++np; }
     if (ina != inb) {
       const int f = id[a] < id[b] ? a : b, s = id[a] < id[b] ? b : a;
       const float t = d[f] / (d[f] - d[s]);
       pc[np] = lerp4(c[f], c[s], t);
       pn[np] = lerp4(n[f], n[s], t);
+      pt[np] = lerp2(uv[f], uv[s], t);
       ++np;
     }
   }
   int cnt = 0;
-  for (int f = 1; f + 1 < np; ++f)
-    cnt += setup_tri<WRITE>(P, S, pc[0], pn[0], pc[f], pn[f], pc[f + 1], pn[f + 1], slot + cnt, col, draw_id, smooth);
+  for (int f = 1; f + 1 < np; ++f) {
+    TexIn ft;
+    ft.t0 = pt[0];
+    ft.t1 = pt[f];
+    ft.t2 = pt[f + 1];
+    ft.node = tx.node;
+    cnt += setup_tri<WRITE>(P, S, pc[0], pn[0], pc[f], pn[f], pc[f + 1], pn[f + 1], slot + cnt, col, draw_id, smooth,
+                            ft);
+  }
   return cnt;
 }
 
@@ -262,12 +297,45 @@ __device__ __forceinline__ int process_tri(const SceneParams& P, const SetupCtx&
   const float4 c2 = vcache[2 * (vbase + i2)], n2 = vcache[2 * (vbase + i2) + 1];
   const float d0 = c0.z + c0.w, d1 = c1.z + c1.w, d2 = c2.z + c2.w;
   if (d0 >= 0.f && d1 >= 0.f && d2 >= 0.f)
-    return setup_tri<WRITE>(P, S, c0, n0, c1, n1, c2, n2, slot, col, draw_id, smooth);
+    return setup_tri<WRITE>(P, S, c0, n0, c1, n1, c2, n2, slot, col, draw_id, smooth, TexIn());
   if (d0 < 0.f && d1 < 0.f && d2 < 0.f) return 0;
   return clip_tri<WRITE>(P, S, c0, n0, c1, n1, c2, n2, i0, i1, i2, slot, col, draw_id, smooth);
 }
 
-// Per-pixel smooth shading of chunk triangle t at pixel centre (px, py).
+// GL bilinear sample with repeat wrap (the sampler Panda3D gives a loaded
+// texture: linear filtering, no mipmaps) at texture coordinates (u, v):
+// texel centres at (i + 0.5) / w, RGBA8 texels read as c / 255.  Every index
+// is wrapped into [0, w) x [0, h), also for infinite or NaN coordinates.
+__device__ __forceinline__ float3 sample_texture(const NodeDesc& nd, float u, float v) {
+  const int w = nd.tex_w, h = nd.tex_h;
+  if (!nd.tex || w <= 0 || h <= 0) return make_float3(1.f, 1.f, 1.f);
+  const float x = fmaf(u - floorf(u), (float)w, -0.5f), y = fmaf(v - floorf(v), (float)h, -0.5f);
+  const float fx = floorf(x), fy = floorf(y);
+  const float ax = x - fx, ay = y - fy;
+  // fx lies in [-1, w - 1]; -1 wraps to w - 1 (fmaxf maps a NaN to -1 as well)
+  int x0 = (int)fminf(fmaxf(fx, -1.f), (float)(w - 1));
+  int y0 = (int)fminf(fmaxf(fy, -1.f), (float)(h - 1));
+  x0 = x0 < 0 ? w - 1 : x0;
+  y0 = y0 < 0 ? h - 1 : y0;
+  const int x1 = x0 + 1 == w ? 0 : x0 + 1, y1 = y0 + 1 == h ? 0 : y0 + 1;
+  const uint32_t* row0 = nd.tex + (long long)y0 * w;
+  const uint32_t* row1 = nd.tex + (long long)y1 * w;
+  const uint32_t t00 = __ldg(row0 + x0), t10 = __ldg(row0 + x1), t01 = __ldg(row1 + x0), t11 = __ldg(row1 + x1);
+  float out[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const int sh = 8 * c;
+    const float c00 = (float)((t00 >> sh) & 255u) / 255.f, c10 = (float)((t10 >> sh) & 255u) / 255.f;
+    const float c01 = (float)((t01 >> sh) & 255u) / 255.f, c11 = (float)((t11 >> sh) & 255u) / 255.f;
+    const float top = (1.f - ax) * c00 + ax * c10, bot = (1.f - ax) * c01 + ax * c11;
+    out[c] = (1.f - ay) * top + ay * bot;
+  }
+  return make_float3(out[0], out[1], out[2]);
+}
+
+// Per-pixel shading of chunk triangle t at pixel centre (px, py): smooth
+// normals and, for textured triangles (flag 16; only when TEX), base = texture(v_uv).
+template <bool TEX = true>
 __device__ __forceinline__ uint32_t shade_smooth(const SceneParams& P, const SetupCtx& S, int t, float px, float py) {
   const float4 e0 = S.T0[t], e1 = S.T1[t], e2 = S.T2[t];
   const float E0 = fmaf(e0.x, px - e0.z, e0.y * (py - e0.w));
@@ -280,7 +348,20 @@ __device__ __forceinline__ uint32_t shade_smooth(const SceneParams& P, const Set
   const float nx = q0 * a0.x + q1 * a1.x + q2 * a2.x;
   const float ny = q0 * a0.y + q1 * a1.y + q2 * a2.y;
   const float nz = q0 * a0.z + q1 * a1.z + q2 * a2.z;
-  return shade_pack(P, nx, ny, nz, S.S3[t]);
+  float4 col = S.S3[t];
+  if (TEX && (__float_as_uint(S.T4[t].y) & 16u)) {
+    // basic.frag:31-32,38: base * v_color.rgb, v_uv interpolated perspective-correct
+    const float4 u01 = S.S4[t], u2n = S.S5[t];
+    const float qs = q0 + q1 + q2;
+    const float iq = qs != 0.f ? 1.f / qs : 0.f;
+    const float u = (q0 * u01.x + q1 * u01.z + q2 * u2n.x) * iq;
+    const float v = (q0 * u01.y + q1 * u01.w + q2 * u2n.y) * iq;
+    const float3 base = sample_texture(P.nodes[__float_as_int(u2n.z)], u, v);
+    col.x = base.x * col.x;
+    col.y = base.y * col.y;
+    col.z = base.z * col.z;
+  }
+  return shade_pack(P, nx, ny, nz, col);
 }
 
 }  // namespace pbr

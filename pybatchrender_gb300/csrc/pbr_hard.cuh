@@ -1,0 +1,408 @@
+// pbr_hard.cuh -- the tile kernel (hard rasteriser) template, instantiated
+// without texture support in pbr_hard.cu and with it in pbr_hard_tex.cu.
+// The pipeline is described at the top of pbr_hard.cu.
+#pragma once
+
+#include "pbr_device.cuh"
+
+namespace pbr {
+
+template <int THREADS, bool PLAIN, bool WINNER, bool TEX>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __grid_constant__ SceneParams P,
+                                                       const __grid_constant__ RasterArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int NW = THREADS / 32;
+  const SmemLayout L = smem_layout(A, THREADS, WINNER);
+  SetupCtx S;
+  S.T0 = reinterpret_cast<float4*>(smem + L.t0);
+  S.T1 = reinterpret_cast<float4*>(smem + L.t1);
+  S.T2 = reinterpret_cast<float4*>(smem + L.t2);
+  S.T3 = reinterpret_cast<float4*>(smem + L.t3);
+  S.T4 = reinterpret_cast<float4*>(smem + L.t4);
+  S.S0 = reinterpret_cast<float4*>(smem + L.s0);
+  S.S1 = reinterpret_cast<float4*>(smem + L.s1);
+  S.S2 = reinterpret_cast<float4*>(smem + L.s2);
+  S.S3 = reinterpret_cast<float4*>(smem + L.s3);
+  S.S4 = reinterpret_cast<float4*>(smem + L.s4);
+  S.S5 = reinterpret_cast<float4*>(smem + L.s5);
+  S.W = (float)P.W;
+  S.H = (float)P.H;
+  S.cull = P.cull;
+  uint32_t* masks = reinterpret_cast<uint32_t*>(smem + L.masks);
+  float4* icache = reinterpret_cast<float4*>(smem + L.icache);
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem + L.state);  // [THREADS * kPx]
+  int* s_scan = reinterpret_cast<int*>(smem + L.misc);
+  float* s_vp = reinterpret_cast<float*>(s_scan + 2 * NW + 8);
+  int* s_item = reinterpret_cast<int*>(s_vp + 16);
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int W = P.W, H = P.H;
+  const int HW = W * H;
+  const int words = A.tri_cap >> 5;
+  const int B = A.bin_px;
+  const int RT = min(THREADS, A.tri_cap >> 1);
+
+  for (int it = 0;; ++it) {
+    int item;
+    if (A.persistent) {
+      if (tid == 0) *s_item = atomicAdd(A.work_counter, 1);
+      __syncthreads();
+      item = *s_item;
+      __syncthreads();
+    } else {
+      item = blockIdx.x + it * gridDim.x;
+    }
+    if (item >= A.num_items) break;
+    const int k = item / A.regions_per_scene;
+    const int r = item - k * A.regions_per_scene;
+    const int p0 = r * A.region_px;
+    const int p1 = min(p0 + A.region_px, HW);
+    const int ry0 = p0 / W, ry1 = (p1 - 1) / W;
+    S.ry0 = (float)ry0;
+    S.ry1 = (float)ry1;
+    if (tid < 16) s_vp[tid] = P.vp[(long long)k * 16 + tid];
+
+    // this thread's 16 pixels: flat indices q0 .. q0+15 of the region
+    const int q0 = p0 + tid * kPx;
+    const int ly = q0 / W, lx = q0 - ly * W;
+    const bool active = q0 < p1;
+
+    // Per-pixel state of the region across chunks.  keys[q - p0] (shared
+    // memory) = depth bits << 32 | (emit order + 1), where emit order counts
+    // the triangles of earlier chunks too: atomicMin keeps the nearest
+    // fragment and, for equal depths, the earliest drawn (order 0 = the
+    // buffer's previous content).  The colour (and winner id) of each of this
+    // lane's 16 pixels stay in registers and are updated after every chunk
+    // for the pixels that chunk won.
+    uint32_t col[kPx];
+    int32_t wid[kPx];
+    int tri_count = 0;
+    unsigned emit_base = 0;  // triangles emitted by earlier chunks
+#pragma unroll
+    for (int j = 0; j < kPx; ++j) {
+      const int q = q0 + j;
+      unsigned long long k0 = (unsigned long long)__float_as_uint(1.f) << 32;
+      col[j] = P.bg_packed;
+      if (PLAIN && q < p1) {
+        k0 = (unsigned long long)(__float_as_uint(A.zbuf[(long long)k * HW + q]) & 0x7fffffffu) << 32;
+        col[j] = A.cbuf[(long long)k * HW + q];
+      }
+      keys[tid * kPx + j] = k0;
+      wid[j] = -1;
+    }
+
+    // ---- K3: pixel-pair raster of the current chunk, then resolve ---------
+    auto flush = [&](bool final_flush) {
+      const int T = tri_count;
+      const int nw = (T + 31) >> 5;
+      const int by_lo = ry0 / B, by_hi = ry1 / B;
+      const int nbins = (by_hi - by_lo + 1) * A.bins_x;
+      for (int i = tid; i < nbins * words; i += THREADS) masks[i] = 0u;
+      __syncthreads();
+      // warp-ballot binner
+      for (int w = warp; w < nw; w += NW) {
+        const int t = w * 32 + lane;
+        int bx0 = 1 << 20, bx1 = -1, by0 = 1 << 20, by1 = -1;
+        if (t < T) {
+          const uint32_t xb = __float_as_uint(S.T3[t].w), yb = __float_as_uint(S.T4[t].x);
+          bx0 = (int)(xb & 0xffffu) / B;
+          bx1 = (int)(xb >> 16) / B;
+          by0 = (int)(yb & 0xffffu) / B - by_lo;
+          by1 = (int)(yb >> 16) / B - by_lo;
+        }
+        const int ux0 = __reduce_min_sync(0xffffffffu, bx0), ux1 = __reduce_max_sync(0xffffffffu, bx1);
+        const int uy0 = __reduce_min_sync(0xffffffffu, by0), uy1 = __reduce_max_sync(0xffffffffu, by1);
+        for (int by = uy0; by <= uy1; ++by)
+          for (int bx = ux0; bx <= ux1; ++bx) {
+            const bool bit = (bx >= bx0) && (bx <= bx1) && (by >= by0) && (by <= by1);
+            const uint32_t m = __ballot_sync(0xffffffffu, bit);
+            if (lane == 0) masks[(by * A.bins_x + bx) * words + w] = m;
+          }
+      }
+      __syncthreads();
+      // bins warp-strided; per bin and mask word, the candidates' (triangle, pixel)
+      // pairs inside the bin are packed 32 per pass (prefix sum of the clipped bbox areas)
+      for (int b = warp; b < nbins; b += NW) {
+        const int bry = b / A.bins_x, bcx = b - bry * A.bins_x;
+        const int bx0 = bcx * B, bx1 = min(bx0 + B, W) - 1;
+        const int by0 = max((by_lo + bry) * B, ry0), by1 = min((by_lo + bry) * B + B - 1, ry1);
+        for (int w = 0; w < nw; ++w) {
+          const uint32_t m = masks[b * words + w];
+          if (m == 0u) continue;
+          int ax0 = 0, ay0 = 0, bw = 1, npx = 0;
+          if ((m >> lane) & 1u) {
+            const int t = w * 32 + lane;
+            const uint32_t xb = __float_as_uint(S.T3[t].w), yb = __float_as_uint(S.T4[t].x);
+            ax0 = max((int)(xb & 0xffffu), bx0);
+            const int ax1 = min((int)(xb >> 16), bx1);
+            ay0 = max((int)(yb & 0xffffu), by0);
+            const int ay1 = min((int)(yb >> 16), by1);
+            const int bh = ay1 - ay0 + 1;
+            bw = ax1 - ax0 + 1;
+            npx = (bw > 0 && bh > 0) ? bw * bh : 0;
+            bw = max(bw, 1);
+          }
+          const float ibw = __fdividef(1.f, (float)bw);
+          int incl = npx;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+          }
+          const int total = __shfl_sync(0xffffffffu, incl, 31);
+          for (int g0 = 0; g0 < total; g0 += 32) {
+            const int g = g0 + lane;
+            int o = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+              const int probe = __shfl_sync(0xffffffffu, incl, o + step - 1);
+              if (probe <= g) o += step;
+            }
+            const int o_start = __shfl_sync(0xffffffffu, incl - npx, o);
+            const int o_ax0 = __shfl_sync(0xffffffffu, ax0, o);
+            const int o_ay0 = __shfl_sync(0xffffffffu, ay0, o);
+            const int o_bw = __shfl_sync(0xffffffffu, bw, o);
+            const float o_ibw = __shfl_sync(0xffffffffu, ibw, o);
+            if (g >= total) continue;
+            const int t = w * 32 + o;
+            const int local = g - o_start;
+            // (local + 0.5) / bw lies at least 0.5 / bw >= 1/64 from an integer
+            const int ry = (int)(((float)local + 0.5f) * o_ibw);
+            const int xx = o_ax0 + local - ry * o_bw, yy = o_ay0 + ry;
+            const int q = yy * W + xx;
+            if (q < p0 || q >= p1) continue;  // the region starts or ends inside a row
+            const float px = (float)xx + 0.5f, py = (float)yy + 0.5f;
+            const float4 e0 = S.T0[t], e1 = S.T1[t], e2 = S.T2[t], zp = S.T3[t];
+            const uint32_t fl = __float_as_uint(S.T4[t].y);
+            const float E0 = fmaf(e0.x, px - e0.z, e0.y * (py - e0.w));
+            const float E1 = fmaf(e1.x, px - e1.z, e1.y * (py - e1.w));
+            const float E2 = fmaf(e2.x, px - e2.z, e2.y * (py - e2.w));
+            const bool in0 = (fl & 1u) ? (E0 >= 0.f) : (E0 > 0.f);
+            const bool in1 = (fl & 2u) ? (E1 >= 0.f) : (E1 > 0.f);
+            const bool in2 = (fl & 4u) ? (E2 >= 0.f) : (E2 > 0.f);
+            if (in0 && in1 && in2) {
+              const float z = fmaxf(fmaf(zp.x, px, fmaf(zp.y, py, zp.z)), 0.f);
+              // z >= 0, so its bits order like the values (the mask folds -0 into +0)
+              const unsigned long long key = ((unsigned long long)(__float_as_uint(z) & 0x7fffffffu) << 32) |
+                                             (unsigned)(emit_base + (unsigned)t + 1u);
+              atomicMin(&keys[q - p0], key);
+            }
+          }
+        }
+      }
+      __syncthreads();
+      // resolve the pixels this chunk won
+      const float py_a = (float)ly + 0.5f;
+#pragma unroll
+      for (int j = 0; j < kPx; ++j) {
+        const uint32_t lo = (uint32_t)keys[tid * kPx + j];
+        if (q0 + j < p1 && lo > emit_base) {
+          const int t = (int)(lo - emit_base) - 1;
+          const float4 meta = S.T4[t];
+          if (__float_as_uint(meta.y) & 8u) {
+            int x = lx + j;
+            float py = py_a;
+            while (x >= W) { x -= W; py += 1.f; }
+            col[j] = shade_smooth<TEX>(P, S, t, (float)x + 0.5f, py);
+          } else {
+            col[j] = __float_as_uint(meta.z);
+          }
+          if (WINNER) wid[j] = __float_as_int(meta.w);
+        }
+      }
+      emit_base += (unsigned)T;
+      if (final_flush && active) {
+        const bool full = (q0 + kPx <= p1);
+        float zb[kPx];
+#pragma unroll
+        for (int j = 0; j < kPx; ++j) zb[j] = __uint_as_float((uint32_t)(keys[tid * kPx + j] >> 32));
+        if (PLAIN) {
+          float* zdst = A.zbuf + (long long)k * HW + q0;
+          uint32_t* cdst = A.cbuf + (long long)k * HW + q0;
+#pragma unroll
+          for (int j = 0; j < kPx; ++j)
+            if (q0 + j < p1) { zdst[j] = zb[j]; cdst[j] = col[j]; }
+        } else {
+          const bool vec = full && ((HW & 15) == 0);
+          for (int c = 0; c < P.C; ++c) {
+            uint8_t* dst = A.out + ((long long)k * P.C + c) * HW + q0;
+            const int sh = 8 * c;
+            if (vec) {
+              uint32_t wv[4];
+#pragma unroll
+              for (int g = 0; g < 4; ++g) {
+                wv[g] = ((col[4 * g + 0] >> sh) & 0xffu) | (((col[4 * g + 1] >> sh) & 0xffu) << 8) |
+                        (((col[4 * g + 2] >> sh) & 0xffu) << 16) | (((col[4 * g + 3] >> sh) & 0xffu) << 24);
+              }
+              *reinterpret_cast<uint4*>(dst) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+            } else {
+#pragma unroll
+              for (int j = 0; j < kPx; ++j)
+                if (q0 + j < p1) dst[j] = (uint8_t)((col[j] >> sh) & 0xffu);
+            }
+          }
+          if (A.depth) {
+            float* dd = A.depth + (long long)k * HW + q0;
+            if (full && ((HW & 3) == 0)) {
+#pragma unroll
+              for (int g = 0; g < 4; ++g)
+                *reinterpret_cast<float4*>(dd + 4 * g) = make_float4(zb[4 * g], zb[4 * g + 1], zb[4 * g + 2], zb[4 * g + 3]);
+            } else {
+#pragma unroll
+              for (int j = 0; j < kPx; ++j)
+                if (q0 + j < p1) dd[j] = zb[j];
+            }
+          }
+          if (WINNER) {
+            int32_t* wd = A.winner + (long long)k * HW + q0;
+#pragma unroll
+            for (int j = 0; j < kPx; ++j)
+              if (q0 + j < p1) wd[j] = wid[j];
+          }
+        }
+      }
+      tri_count = 0;
+      __syncthreads();
+    };
+
+    // ---- K1 / K2: walk nodes and instances in draw order -----------------
+    // Instance batches of up to icap instances (model matrices in shared
+    // memory); then rounds of THREADS source triangles, one per thread: the
+    // thread transforms its triangle's three vertices itself (no vertex cache,
+    // no per-instance barriers), culls and rejects triangles that cover no
+    // pixel centre, and the survivors are compacted in draw order with one
+    // barrier per round (warp prefix sums + per-warp totals in shared memory).
+    __syncthreads();  // s_vp visible
+    const float vp0 = s_vp[0], vp1 = s_vp[1], vp2 = s_vp[2], vp3 = s_vp[3];
+    const float vp4 = s_vp[4], vp5 = s_vp[5], vp6 = s_vp[6], vp7 = s_vp[7];
+    const float vp8 = s_vp[8], vp9 = s_vp[9], vp10 = s_vp[10], vp11 = s_vp[11];
+    const float vp12 = s_vp[12], vp13 = s_vp[13], vp14 = s_vp[14], vp15 = s_vp[15];
+    int parity = 0;
+    for (int n = A.node_begin; n < A.node_end; ++n) {
+      const NodeDesc& nd = P.nodes[n];
+      const MeshDesc& me = P.meshes[nd.mesh];
+      int cnt = nd.counts ? nd.counts[k] : nd.ips;
+      cnt = max(0, min(cnt, nd.ips));
+      const int nt = me.nt;
+      if (cnt == 0 || nt == 0) continue;
+      const bool textured = TEX && nd.tex != nullptr;  // textured triangles are shaded per pixel
+      const bool smooth = me.smooth != 0 || textured;
+      for (int b0 = 0; b0 < cnt; b0 += A.icap) {
+        const int nbc = min(A.icap, cnt - b0);
+        __syncthreads();  // the previous batch's triangles are done with icache
+        for (int i = tid; i < nbc; i += THREADS) {
+          const long long id = nd.shared ? (long long)(b0 + i) : (long long)k * nd.ips + b0 + i;
+          float m[12];
+          build_model(nd, id, m);
+          if (r == 0) write_back_bound(nd, id);
+          icache[i * 4 + 0] = make_float4(m[0], m[1], m[2], m[3]);
+          icache[i * 4 + 1] = make_float4(m[4], m[5], m[6], m[7]);
+          icache[i * 4 + 2] = make_float4(m[8], m[9], m[10], m[11]);
+          const float* cc = nd.color + id * 4;
+          icache[i * 4 + 3] = make_float4(cc[0], cc[1], cc[2], cc[3]);
+        }
+        __syncthreads();
+        const int total_t = nbc * nt;
+        for (int t0 = 0; t0 < total_t; t0 += RT) {
+          // up to 2 emitted triangles per source triangle (near-plane clip)
+          const int rem = min(RT, total_t - t0);
+          if (tri_count + 2 * rem > A.tri_cap) flush(false);
+          int c = 0, li = 0, ti = 0, i0 = 0, i1 = 0, i2 = 0;
+          float4 cv[3];
+          SV sv[3];
+          bool front = false;
+          if (tid < rem) {
+            const int t = t0 + tid;
+            li = t / nt;
+            ti = t - li * nt;
+            i0 = me.idx[3 * ti];
+            i1 = me.idx[3 * ti + 1];
+            i2 = me.idx[3 * ti + 2];
+            const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
+            const int iv[3] = {i0, i1, i2};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const int vi = iv[q];
+              const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
+              const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
+              const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
+              const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
+              cv[q].x = vp0 * wx + vp1 * wy + vp2 * wz + vp3;
+              cv[q].y = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
+              cv[q].z = vp8 * wx + vp9 * wy + vp10 * wz + vp11;
+              cv[q].w = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
+            }
+            const float d0 = cv[0].z + cv[0].w, d1 = cv[1].z + cv[1].w, d2 = cv[2].z + cv[2].w;
+            front = d0 >= 0.f && d1 >= 0.f && d2 >= 0.f;
+            const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (front) {
+#pragma unroll
+              for (int q = 0; q < 3; ++q) sv[q] = to_screen(cv[q], S.W, S.H);
+              c = setup_tri_sv<false>(P, S, sv[0], z4, sv[1], z4, sv[2], z4, 0, z4, 0, smooth);
+            } else if (!(d0 < 0.f && d1 < 0.f && d2 < 0.f)) {
+              c = clip_tri<false>(P, S, cv[0], z4, cv[1], z4, cv[2], z4, i0, i1, i2, 0, z4, 0, smooth);
+            }
+          }
+          // draw-order compaction: warp prefix sum, then the totals of the warps before this one
+          int incl = c;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          int* wcnt = s_scan + parity * NW;
+          if (lane == 31) wcnt[warp] = incl;
+          __syncthreads();
+          int before = 0, total = 0;
+#pragma unroll
+          for (int w = 0; w < NW; ++w) {
+            const int v = wcnt[w];
+            before += w < warp ? v : 0;
+            total += v;
+          }
+          parity ^= 1;
+          if (c > 0) {
+            const int slot = tri_count + before + incl - c;
+            const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
+            const float4 col = icache[li * 4 + 3];
+            const int draw_id = (nd.rank_base + b0 + li) * P.max_tris + ti;
+            // world normals: the provoking vertex's for flat meshes (the three are identical), all three if smooth
+            float4 nv[3];
+            const int iv[3] = {i0, i1, i2};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              if (q == 0 || smooth) {
+                const int vi = iv[q];
+                const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
+                const float nx = r0.x * ax + r0.y * ay + r0.z * az;
+                const float ny = r1.x * ax + r1.y * ay + r1.z * az;
+                const float nz = r2.x * ax + r2.y * ay + r2.z * az;
+                const float l2 = nx * nx + ny * ny + nz * nz;
+                const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
+                nv[q] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
+              } else {
+                nv[q] = nv[0];
+              }
+            }
+            TexIn tx;
+            if (textured) {
+              tx.t0 = mesh_uv(me, i0);
+              tx.t1 = mesh_uv(me, i1);
+              tx.t2 = mesh_uv(me, i2);
+              tx.node = n;
+            }
+            if (front)
+              setup_tri_sv<true>(P, S, sv[0], nv[0], sv[1], nv[1], sv[2], nv[2], slot, col, draw_id, smooth, tx);
+            else
+              clip_tri<true>(P, S, cv[0], nv[0], cv[1], nv[1], cv[2], nv[2], i0, i1, i2, slot, col, draw_id, smooth,
+                             tx);
+          }
+          tri_count += total;
+        }
+      }
+    }
+    flush(true);
+  }
+}
+
+}  // namespace pbr

@@ -28,6 +28,7 @@ struct MeshDesc {
   const float* pos;    // [nv,3]
   const float* nrm;    // [nv,3]
   const int32_t* idx;  // [nt,3]
+  const float* uv;     // [nv,2] texture coordinates, or null (all 0)
   int32_t nv, nt, smooth, pad;
 };
 
@@ -41,8 +42,11 @@ struct NodeDesc {
   float* grot;            // d/d(heading, pitch, roll)
   float* gscale;
   float* gcol;
+  // texture (shaders/basic.frag:31-32): [tex_h, tex_w] RGBA8 texels, row 0 at
+  // v = 0 (the bottom row of the image); null when the node is untextured
+  const uint32_t* tex;
   int32_t mesh, ips, shared, mode;
-  int32_t rank_base, pad0, pad1, pad2;
+  int32_t rank_base, tex_w, tex_h, pad0;
   // state binding: position component c (0..2) / HPR angle c (3..5) of buffer
   // row r is src[r * src_stride + src_col[c]] when src is set and src_col[c] >= 0
   const float* src;
@@ -80,7 +84,8 @@ struct RasterArgs {
   int32_t region_px, regions_per_scene, num_items;
   int32_t max_region_bins;
   int32_t persistent;
-  int32_t smooth_any;
+  int32_t smooth_any;  // per-pixel shading records S0..S3 (smooth meshes or textured nodes)
+  int32_t tex_any;     // texture-coordinate records S4, S5 (textured nodes)
   int32_t multi_chunk;
 };
 
@@ -109,6 +114,7 @@ struct SoftLayout {
 struct SmemLayout {
   int t0, t1, t2, t3, t4;  // float4 [tri_cap]: three edges, depth plane + x-box, meta
   int s0, s1, s2, s3;      // float4 [tri_cap]: smooth-shading attributes (if smooth_any)
+  int s4, s5;              // float4 [tri_cap]: texture coordinates + node (if tex_any)
   int masks;               // uint32 [max_region_bins * tri_cap/32]
   int vcache;              // float4 [vcap*2]: clip position, world normal
   int icache;              // float4 [icap*4]: model matrix rows, colour
@@ -135,6 +141,12 @@ __host__ __device__ inline SmemLayout smem_layout(const RasterArgs& a, int threa
     L.s3 = off; off += align16(t4);
   } else {
     L.s0 = L.s1 = L.s2 = L.s3 = 0;
+  }
+  if (a.tex_any) {
+    L.s4 = off; off += align16(t4);
+    L.s5 = off; off += align16(t4);
+  } else {
+    L.s4 = L.s5 = 0;
   }
   L.masks = off; off += align16(a.max_region_bins * (a.tri_cap / 32) * 4);
   L.vcache = off; off += align16(a.vcap * 32);

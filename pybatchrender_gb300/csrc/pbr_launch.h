@@ -10,8 +10,10 @@ namespace pbr {
 
 // Hard raster (pbr_hard.cu).  threads in {128, 256, 512}; plain selects the
 // per-node variant that reads/writes the global depth/colour buffer.
-cudaError_t hard_set_smem_limit(int threads, bool plain, bool winner, int bytes);
-cudaError_t hard_occupancy(int threads, bool plain, bool winner, int smem_bytes, int* blocks_per_sm);
+cudaError_t hard_set_smem_limit(int threads, bool plain, bool winner, bool tex, int bytes);
+cudaError_t hard_occupancy(int threads, bool plain, bool winner, bool tex, int smem_bytes, int* blocks_per_sm);
+// the textured instantiation of the tile kernel (pbr_hard_tex.cu); null for an unsupported combination
+const void* hard_tex_fn(int threads, bool plain, bool winner);
 cudaError_t hard_launch(int threads, bool plain, bool winner, const SceneParams& P, const RasterArgs& A,
                         int grid, int smem_bytes, cudaStream_t stream);
 // Scene-per-warp raster (pbr_small.cu); blocks of small_warps() warps.

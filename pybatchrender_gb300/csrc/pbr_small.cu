@@ -50,7 +50,7 @@ struct SmallLayout {
 };
 
 // Per-warp shared memory.  Triangle records T0..T4 (and S0..S3 for smooth
-// shading); bgrec is a T4-shaped record just before T4[0] holding the
+// shading; textured scenes take the tile kernel); bgrec is a T4-shaped record just before T4[0] holding the
 // background colour (.z) and winner -1 (.w), so that draw order + 1 indexes
 // both.  The setup stage's vertex cache (3 float4 per vertex: clip position;
 // normal with .w = z + w; screen position), instance table (5 float4 per
@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
   S.S1 = reinterpret_cast<float4*>(base + L.s1);
   S.S2 = reinterpret_cast<float4*>(base + L.s2);
   S.S3 = reinterpret_cast<float4*>(base + L.s3);
+  S.S4 = S.S5 = nullptr;  // no textured triangles in this kernel
   S.W = (float)W;
   S.H = (float)H;
   S.ry0 = 0.f;
@@ -447,10 +448,10 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
               const int j = 4 * g + q;
               const uint32_t r = klo[64 * j];
               const float4* rec = reinterpret_cast<const float4*>(rec4 + 16 * r);
-              if (PLAIN) {
-                col[q] = r ? __float_as_uint(rec->z) : A.cbuf[lane_pix + boff + j];
+              if (PLAIN && r == 0) {
+                col[q] = A.cbuf[lane_pix + boff + j];
               } else if (SMOOTH && (__float_as_uint(rec->y) & 8u)) {
-                col[q] = shade_smooth(P, S, (int)r - 1, (float)(col0 + seg_x + j) + 0.5f, (float)(row0 + seg_r) + 0.5f);
+                col[q] = shade_smooth<false>(P, S, (int)r - 1, (float)(col0 + seg_x + j) + 0.5f, (float)(row0 + seg_r) + 0.5f);
               } else {
                 col[q] = __float_as_uint(rec->z);
               }

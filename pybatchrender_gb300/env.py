@@ -189,6 +189,78 @@ class PBREnv(_Base):
             raise RuntimeError("Renderer is not initialized. Construct env with a renderer and pass it to PBREnv.")
         return self._renderer.step(obs)
 
+    # ------------------------------------------------------------ snapshots
+    def _is_secondary_worker(self) -> bool:
+        return int(getattr(self.cfg, "num_workers", 1) or 1) > 1 and int(getattr(self.cfg, "worker_index", 0) or 0) != 0
+
+    @staticmethod
+    def _snapshot_path(out_dir: str | None, prefix: str, ext: str):
+        import random
+        import time
+        from pathlib import Path
+        out = Path(out_dir) if out_dir is not None else Path(".")
+        out.mkdir(parents=True, exist_ok=True)
+        name = f"{prefix}_{time.strftime('%Y%m%d_%H%M%S')}_{random.randint(0, 999999):06d}.{ext}"
+        return (out / name).resolve()
+
+    def _make_grid_frame(self, pixels: torch.Tensor, indices: list[int] | None = None, num: int = 16,
+                         scale: int = 1):
+        """Grid image of the batch (``env.py:186-241``)."""
+        from .imagefile import make_grid
+        return make_grid(pixels, indices, num, scale)
+
+    def save_batch_examples(self, *, pixels: torch.Tensor | None = None, obs: torch.Tensor | None = None,
+                            indices: list[int] | None = None, num: int = 16, scale: int = 1,
+                            out_dir: str | None = "./outputs", filename_prefix: str = "batch_example",
+                            return_bytes: bool = False):
+        """Save one PNG grid of batch elements (``env.py:97-184``); returns the
+        path, or ``(path, png_bytes)`` when ``return_bytes``.  Worker processes
+        other than worker 0 return None."""
+        from .imagefile import encode_png
+        if self._is_secondary_worker():
+            return None
+        if pixels is None:
+            pixels = self.render_pixels(obs)
+        if pixels is None:
+            raise RuntimeError("No pixels available to save.")
+        data = encode_png(self._make_grid_frame(pixels, indices, num, scale))
+        path = self._snapshot_path(out_dir, filename_prefix, "png")
+        path.write_bytes(data)
+        return (str(path), data) if return_bytes else str(path)
+
+    def save_batch_gif(self, *, num_steps: int = 100, frame_interval: int = 2, indices: list[int] | None = None,
+                       num: int = 16, scale: int = 2, duration_ms: int = 100, out_dir: str | None = "./outputs",
+                       filename_prefix: str = "batch_animation", return_bytes: bool = False):
+        """Reset, run ``num_steps`` random-action steps and save an animated GIF
+        of the batch grid, one frame every ``frame_interval`` steps
+        (``env.py:243-358``)."""
+        from .imagefile import encode_gif
+        if self._is_secondary_worker():
+            return None
+        frames = []
+        td = self._reset()
+        pixels = td.get("pixels", None)
+        if pixels is None:
+            pixels = self.render_pixels(td.get("observation", None))
+        if pixels is not None:
+            frames.append(self._make_grid_frame(pixels, indices, num, scale))
+        for step in range(1, int(num_steps) + 1):
+            td["action"] = self.action_spec.rand()
+            td = self.step(td)
+            td = td["next"]
+            if step % int(frame_interval) == 0:
+                pixels = td.get("pixels", None)
+                if pixels is None:
+                    pixels = self.render_pixels(td.get("observation", None))
+                if pixels is not None:
+                    frames.append(self._make_grid_frame(pixels, indices, num, scale))
+        if not frames:
+            raise RuntimeError("No frames captured. Ensure rendering is enabled.")
+        data = encode_gif(frames, duration_ms=duration_ms, loop=0)
+        path = self._snapshot_path(out_dir, filename_prefix, "gif")
+        path.write_bytes(data)
+        return (str(path), data) if return_bytes else str(path)
+
     @classmethod
     def make_parallel_env(cls, *, config: PBRConfig, renderer_cls, num_workers: int,
                           mp_start_method: str = "spawn", shared_memory: bool = True):

@@ -31,6 +31,9 @@ class Mesh:
     indices: ``[nt,3]`` int32, counter-clockwise when seen from the outside.
     ``smooth`` is False when every triangle's three vertex normals are
     identical (flat shading: a triangle is lit with its first vertex's normal).
+    ``uvs``: ``[nv,2]`` float32 texture coordinates (GL convention, ``v = 0`` at
+    the bottom of the image) or None; ``texture``: the model's own texture,
+    ``[h,w,4]`` uint8 RGBA in image order, or None.
     """
 
     positions: np.ndarray
@@ -38,6 +41,8 @@ class Mesh:
     indices: np.ndarray
     name: str = "mesh"
     smooth: bool = field(default=False)
+    uvs: np.ndarray | None = None
+    texture: np.ndarray | None = None
 
     def __post_init__(self) -> None:
         self.positions = np.ascontiguousarray(self.positions, dtype=np.float32).reshape(-1, 3)
@@ -47,6 +52,10 @@ class Mesh:
             raise ValueError("positions and normals must have the same shape")
         if self.indices.size and (self.indices.min() < 0 or self.indices.max() >= len(self.positions)):
             raise ValueError("mesh indices out of range")
+        if self.uvs is not None:
+            self.uvs = np.ascontiguousarray(self.uvs, dtype=np.float32).reshape(-1, 2)
+            if self.uvs.shape[0] != self.positions.shape[0]:
+                raise ValueError("uvs must have one row per vertex")
         tri_n = self.normals[self.indices]  # [nt,3,3]
         self.smooth = bool(np.any(tri_n != tri_n[:, :1, :]))
 
@@ -62,7 +71,8 @@ class Mesh:
         return self.positions.min(axis=0), self.positions.max(axis=0)
 
     def copy(self) -> "Mesh":
-        return Mesh(self.positions.copy(), self.normals.copy(), self.indices.copy(), self.name)
+        return Mesh(self.positions.copy(), self.normals.copy(), self.indices.copy(), self.name,
+                    uvs=None if self.uvs is None else self.uvs.copy(), texture=self.texture)
 
 
 # ---------------------------------------------------------------------------
@@ -70,7 +80,8 @@ class Mesh:
 # ---------------------------------------------------------------------------
 
 def unit_cube() -> Mesh:
-    """Unit cube on ``[0,1]^3``: 6 faces x 4 vertices, 12 triangles, face normals."""
+    """Unit cube on ``[0,1]^3``: 6 faces x 4 vertices, 12 triangles, face
+    normals; each face maps the whole texture, (0,0) at its origin corner."""
     # (normal, origin corner, edge u, edge v) with u x v == normal so that
     # (o, o+u, o+u+v) and (o, o+u+v, o+v) wind counter-clockwise seen from outside.
     faces = [
@@ -81,16 +92,17 @@ def unit_cube() -> Mesh:
         ((0, 0, 1), (0, 0, 1), (1, 0, 0), (0, 1, 0)),
         ((0, 0, -1), (0, 1, 0), (1, 0, 0), (0, -1, 0)),
     ]
-    pos, nrm, idx = [], [], []
+    pos, nrm, idx, uvs = [], [], [], []
     for n, o, u, v in faces:
         o, u, v = np.array(o, float), np.array(u, float), np.array(v, float)
         assert np.allclose(np.cross(u, v), n)
         base = len(pos)
-        for corner in (o, o + u, o + u + v, o + v):
+        for corner, uv in ((o, (0, 0)), (o + u, (1, 0)), (o + u + v, (1, 1)), (o + v, (0, 1))):
             pos.append(corner)
             nrm.append(n)
+            uvs.append(uv)
         idx += [(base, base + 1, base + 2), (base, base + 2, base + 3)]
-    return Mesh(np.array(pos), np.array(nrm), np.array(idx), name="box")
+    return Mesh(np.array(pos), np.array(nrm), np.array(idx), name="box", uvs=np.array(uvs))
 
 
 def cylinder(segments: int = 64, radius: float = 0.5, height: float = 1.0) -> Mesh:
@@ -183,14 +195,18 @@ def _triangulate_fan(poly: Sequence[int]) -> list[tuple[int, int, int]]:
 
 def load_egg(path: str) -> Mesh:
     """Minimal Panda3D ``.egg`` reader: one ``<VertexPool>`` of ``<Vertex>``
-    entries (position + optional ``<Normal>``) and ``<Polygon>`` entries with
-    ``<VertexRef>``.  Polygons are fan-triangulated; vertices without a normal
-    get the polygon's face normal."""
+    entries (position + optional ``<Normal>`` and ``<UV>``) and ``<Polygon>``
+    entries with ``<VertexRef>``.  Polygons are fan-triangulated; vertices
+    without a normal get the polygon's face normal.  The first ``<Texture>``
+    whose image file exists (PNG) becomes the mesh's own texture."""
     import re
+
+    from .textures import load_image
 
     text = open(path, "r", encoding="utf-8").read()
     pos: dict[int, tuple[float, float, float]] = {}
     nrm: dict[int, tuple[float, float, float]] = {}
+    uvs: dict[int, tuple[float, float]] = {}
     for m in re.finditer(r"<Vertex>\s*(\d+)\s*\{([^{}]*(?:\{[^{}]*\}[^{}]*)*)\}", text):
         vid = int(m.group(1))
         body = m.group(2)
@@ -199,11 +215,20 @@ def load_egg(path: str) -> Mesh:
         nm = re.search(r"<Normal>\s*\{([^}]*)\}", body)
         if nm:
             nrm[vid] = tuple(float(x) for x in nm.group(1).split()[:3])
+        um = re.search(r"<UV>\s*(?:\w+\s*)?\{([^}]*)\}", body)
+        if um:
+            uvs[vid] = tuple(float(x) for x in um.group(1).split()[:2])
+    texture = None
+    for m in re.finditer(r"<Texture>\s*\S*\s*\{\s*\"?([^\"<}\s]+)\"?", text):
+        tex_path = os.path.join(os.path.dirname(path), m.group(1))
+        if os.path.isfile(tex_path) and tex_path.lower().endswith(".png"):
+            texture = load_image(tex_path)
+            break
     polys = []
     for m in re.finditer(r"<Polygon>\s*\{(.*?)<VertexRef>\s*\{([^}]*)\}", text, re.S):
         refs = [int(x) for x in m.group(2).split("<")[0].split()]
         polys.append(refs)
-    out_p, out_n, out_i = [], [], []
+    out_p, out_n, out_i, out_uv = [], [], [], []
     for refs in polys:
         pts = np.array([pos[r] for r in refs], float)
         fn = np.cross(pts[1] - pts[0], pts[2] - pts[0])
@@ -213,16 +238,23 @@ def load_egg(path: str) -> Mesh:
         for r in refs:
             out_p.append(pos[r])
             out_n.append(nrm.get(r, tuple(fn)))
+            out_uv.append(uvs.get(r, (0.0, 0.0)))
         out_i += _triangulate_fan(list(range(base, base + len(refs))))
     n = np.array(out_n, float)
     n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-12)
-    return Mesh(np.array(out_p), n, np.array(out_i), name=os.path.basename(path))
+    return Mesh(np.array(out_p), n, np.array(out_i), name=os.path.basename(path),
+                uvs=np.array(out_uv) if uvs else None, texture=texture)
 
 
 def load_gltf(path: str) -> Mesh:
     """Minimal glTF 2.0 reader: first primitive of the first mesh (triangles),
-    POSITION / NORMAL float accessors and an index accessor, data in an
-    external ``.bin`` buffer."""
+    POSITION / NORMAL / TEXCOORD_0 float accessors and an index accessor, data
+    in an external ``.bin`` buffer.  glTF puts ``v = 0`` at the top of the
+    image; the coordinates are flipped (``v -> 1 - v``) to the GL convention,
+    as Panda3D's glTF loader does.  A PNG ``baseColorTexture`` of the
+    primitive's material becomes the mesh's own texture."""
+    from .textures import load_image
+
     with open(path, "r", encoding="utf-8") as f:
         doc = json.load(f)
     base = os.path.dirname(path)
@@ -261,7 +293,21 @@ def load_gltf(path: str) -> Mesh:
         for k in range(3):
             np.add.at(n, idx[:, k], fn)
     n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-12)
-    return Mesh(p, n, idx.astype(np.int32), name=os.path.basename(path))
+    uv = None
+    if "TEXCOORD_0" in prim["attributes"]:
+        t = accessor(prim["attributes"]["TEXCOORD_0"]).astype(np.float32)
+        uv = np.stack([t[:, 0], 1.0 - t[:, 1]], axis=1)
+    texture = None
+    try:
+        mat = doc["materials"][prim["material"]]
+        tex = doc["textures"][mat["pbrMetallicRoughness"]["baseColorTexture"]["index"]]
+        uri = doc["images"][tex["source"]]["uri"]
+        tex_path = os.path.join(base, uri)
+        if os.path.isfile(tex_path) and tex_path.lower().endswith(".png"):
+            texture = load_image(tex_path)
+    except (KeyError, IndexError, TypeError):
+        pass
+    return Mesh(p, n, idx.astype(np.int32), name=os.path.basename(path), uvs=uv, texture=texture)
 
 
 _BUILTIN = {
@@ -414,4 +460,4 @@ def bake(mesh: Mesh, model_scale=None, model_hpr=None, pivot_relative_point=None
         p = p - (lo + (hi - lo) * rel)
     out.positions = p.astype(np.float32)
     out.normals = n.astype(np.float32)
-    return Mesh(out.positions, out.normals, out.indices, mesh.name)
+    return Mesh(out.positions, out.normals, out.indices, mesh.name, uvs=out.uvs, texture=out.texture)

@@ -20,8 +20,10 @@ Differences from the reference, all deliberate:
 * A shared node with ``1 < I < num_scenes`` draws instance i of every scene from
   row i.  The reference sets ``instancesPerScene = max(1, B // N)`` (``node.py:90``),
   which is 1 in that case and makes every instance decode as its own scene.
-* ``texture`` other than None raises NotImplementedError (``useTexture`` is 0 in
-  every reference scene; textured drawing is not part of this renderer yet).
+* ``texture`` also accepts an image array or tensor, and ``True`` falls back to
+  a white texture when the model brings none (the reference leaves that case to
+  whatever Panda3D binds).  Textured nodes are drawn in the hard raster modes;
+  the soft (differentiable) mode rejects them.
 """
 from __future__ import annotations
 
@@ -34,6 +36,7 @@ import torch
 
 from .meshes import Mesh, bake, resolve_model
 from .shader_context import PBRShaderContext
+from .textures import WHITE, as_rgba8, gl_rows, load_image
 
 MODE_HPR, MODE_ROT, MODE_MAT = 0, 1, 2
 
@@ -73,6 +76,7 @@ class PBRNode(PBRShaderContext):
         self.model_scale_units = model_scale_units
         self.name = name
         self.device = getattr(showbase, "state_device", torch.device("cpu"))
+        self.texture: np.ndarray | None = None  # [h,w,4] uint8 RGBA, row 0 at v = 0
 
         if model_path:
             self.mesh: Mesh | None = bake(resolve_model(model_path), model_scale, model_hpr,
@@ -218,9 +222,28 @@ class PBRNode(PBRShaderContext):
 
     # ----------------------------------------------------------------- misc
     def set_texture(self, texture=None) -> None:
-        if texture is not None and texture is not False:
-            raise NotImplementedError("textured nodes are not supported by the GB300 renderer (useTexture = 0 only)")
-        self._set_shader_input('useTexture', 0.0)
+        """``useTexture`` and ``p3d_Texture0`` (``renderer/node.py:277-287``).
+
+        ``texture``: a PNG path (or ``.npy``), an image array / tensor
+        ``[h,w]`` or ``[h,w,1|3|4]`` (uint8, or float in [0,1]; row 0 = top),
+        ``True`` for the model's own texture (white if it has none), or
+        None / False for no texture."""
+        if texture is None or texture is False:
+            self.texture = None
+            self._set_shader_input('useTexture', 0.0)
+        else:
+            if texture is True:
+                own = self.mesh.texture if self.mesh is not None else None
+                img = own if own is not None else WHITE
+            elif isinstance(texture, str):
+                img = load_image(texture)
+            else:
+                img = as_rgba8(texture)
+            self.texture = gl_rows(img)
+            self._set_shader_input('useTexture', 1.0)
+        changed = getattr(self.base, "_texture_changed", None)
+        if changed is not None:
+            changed(self)
 
     def reparent_to(self, parent) -> None:
         raise NotImplementedError("PBRNode.reparent_to is not implemented yet")
@@ -261,10 +284,12 @@ class PBRNode(PBRShaderContext):
             "counts": None if self.counts is None else self.counts.detach().cpu().numpy(),
             "pos": pos.detach().cpu().numpy(), "rot": rot.detach().cpu().numpy(),
             "scale": scale.detach().cpu().numpy(), "color": color.detach().cpu().numpy(),
+            "texture": self.texture,
         }
 
 
 def mesh_key(mesh: Mesh) -> bytes:
     """Content key used to share identical baked meshes between nodes."""
     return (mesh.positions.tobytes() + b"|" + mesh.normals.tobytes() + b"|" + mesh.indices.tobytes()
+            + b"|" + (mesh.uvs.tobytes() if mesh.uvs is not None else b"-")
             + np.int64(mesh.num_vertices).tobytes())

@@ -282,6 +282,8 @@ class PBRRenderer:
         autograd is enabled and a node tensor (``pos``, ``hpr``, ``scale``,
         ``color``) or ``light_dir`` requires grad."""
         from .soft import soft_params, soft_render
+        if any(n.texture is not None for n in self.geometry_nodes()):
+            raise NotImplementedError("textured nodes are drawn by the hard raster modes only (soft mode: untextured)")
         self._require_ready()
         params = soft_params(self)
         if torch.is_grad_enabled() and (any(p.requires_grad for p in params)
@@ -489,12 +491,17 @@ class PBRRenderer:
                     mid = ctypes.c_int()
                     _capi.call(lib, ctx, "pbr_mesh_register", _capi.ptr(pos), _capi.ptr(nrm), _capi.ptr(idx),
                                m.num_vertices, m.num_triangles, int(m.smooth), ctypes.byref(mid))
+                    if m.uvs is not None:
+                        uv = torch.from_numpy(m.uvs).to(self.device)
+                        self._mesh_tensors.append((uv,))
+                        _capi.call(lib, ctx, "pbr_mesh_set_uv", mid.value, _capi.ptr(uv))
                     mesh_ids[key] = mid.value
                 nid = ctypes.c_int()
                 _capi.call(lib, ctx, "pbr_node_add", mesh_ids[key], node.instances_per_scene,
                            int(node.shared_across), ctypes.byref(nid))
                 self._node_ids[node] = nid.value
                 self._bind_node_buffers(node)
+                self._bind_node_texture(node)
             for node, comp, col in self._state_bindings:
                 if node in self._node_ids:
                     _capi.call(lib, ctx, "pbr_node_bind_state", self._node_ids[node], comp, col)
@@ -523,6 +530,23 @@ class PBRRenderer:
         mode, pos, rot, scale, color = node.kernel_buffers()
         _capi.call(self._lib, self._ctx, "pbr_node_set_buffers", nid, mode, _capi.ptr(pos), _capi.ptr(rot),
                    _capi.ptr(scale), _capi.ptr(color), _capi.ptr(counts))
+
+    def _bind_node_texture(self, node: PBRNode) -> None:
+        nid = self._node_ids[node]
+        self._tex_tensors = getattr(self, "_tex_tensors", {})
+        if node.texture is None:
+            self._tex_tensors.pop(nid, None)
+            _capi.call(self._lib, self._ctx, "pbr_node_set_texture", nid, None, 0, 0)
+            return
+        tex = torch.from_numpy(node.texture).to(self.device)
+        self._tex_tensors[nid] = tex
+        _capi.call(self._lib, self._ctx, "pbr_node_set_texture", nid, _capi.ptr(tex), int(tex.shape[1]),
+                   int(tex.shape[0]))
+
+    def _texture_changed(self, node: PBRNode) -> None:
+        if self._ctx is not None and node in getattr(self, "_node_ids", {}):
+            self._bind_node_texture(node)
+            self._graph = None
 
     def _rebind_node(self, node: PBRNode) -> None:
         if self._ctx is not None and node in getattr(self, "_node_ids", {}):

@@ -64,8 +64,8 @@ def test_node_setter_semantics():
     assert s.buf_instances == 2
     with pytest.raises(NotImplementedError):
         r.add_node("models/box", 1, backend="loop")
-    with pytest.raises(NotImplementedError):
-        r.add_node("models/box", 1, texture="tex.png")
+    with pytest.raises(FileNotFoundError):
+        r.add_node("models/box", 1, texture="no_such_texture.png")
     with warnings.catch_warnings(record=True) as w:
         warnings.simplefilter("always")
         r.add_node("models/box", 1, positions=torch.zeros(3))

@@ -296,3 +296,22 @@ def test_steering_env_renders_and_matches_oracle(cuda, oracle):
     first = env._renderer.sphere_node
     env.reset()
     assert env._renderer.sphere_node is not first and first not in env._renderer.geometry_nodes()
+
+
+def test_save_batch_snapshots(cuda, tmp_path):
+    """save_batch_examples / save_batch_gif on rendered CartPole frames."""
+    from pybatchrender_gb300.imagefile import make_grid
+    from pybatchrender_gb300.renderer import textures
+    from tests.test_imagefile_cpu import _gif_decode
+
+    env = pbr.envs.make("CartPole-v0", num_scenes=9)
+    td = env.reset()
+    path, data = env.save_batch_examples(pixels=td["pixels"], num=9, scale=2, out_dir=str(tmp_path),
+                                         return_bytes=True)
+    img = textures.decode_png(data)
+    assert np.array_equal(img[..., :3], make_grid(td["pixels"], num=9, scale=2))
+    path, data = env.save_batch_gif(num_steps=6, frame_interval=3, num=4, scale=1, out_dir=str(tmp_path),
+                                    return_bytes=True)
+    frames, delays, loop = _gif_decode(data)
+    assert len(frames) == 3 and frames[0].shape == (128, 128, 3) and loop == 0
+    assert frames[0].max() > 0

@@ -236,6 +236,26 @@ int pbr_debug_transforms(pbr_ctx* ctx, int node_id, float* d_out, void* stream);
  * context's device, then clears them).  0 = none. */
 int pbr_device_status(pbr_ctx* ctx, int32_t* out_flags);
 
+/* One CartPole-v0 step for n scenes in a single launch (no context needed):
+ * the Euler-integrated dynamics, termination, survival reward and auto-reset
+ * of envs/cartpole/env.py:111-218 (_dynamics, _termination, _reward and the
+ * auto-reset of _step), evaluated with the same float32 roundings as the
+ * reference's tensor operations.
+ *   d_obs [n,4] (x, x_dot, theta, theta_dot), d_action [n] int64 (1 = push
+ *   right), d_step_count [n] int64 or NULL (all 0);
+ *   d_reset_* [n] float32 each: the initial states to use where a scene is done
+ *   (required when auto_reset);
+ *   outputs: d_next_raw [n,4] (the state after the dynamics: what is drawn),
+ *   d_next_obs [n,4] (after auto-reset), d_reward [n], d_done [n] bool bytes,
+ *   d_next_step_count [n] int64.  The [n,4] arrays are 16-byte aligned.
+ *   consts: gravity, masscart, masspole, length, force_mag, tau, x_threshold,
+ *   theta_threshold (radians), max_steps. */
+int pbr_cartpole_step(const float* d_obs, const int64_t* d_action, const int64_t* d_step_count,
+                      const float* d_reset_x, const float* d_reset_x_dot, const float* d_reset_theta,
+                      const float* d_reset_theta_dot, float* d_next_raw, float* d_next_obs, float* d_reward,
+                      uint8_t* d_done, int64_t* d_next_step_count, long long n, const double* consts,
+                      int auto_reset, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

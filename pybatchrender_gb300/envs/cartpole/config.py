@@ -13,6 +13,7 @@ class CartPoleConfig(PBRConfig):
     action_type: str = "discrete"
     max_steps: int = 500
     auto_reset: bool = True
+    fused_step: bool = True  # on CUDA: the step's arithmetic as one fused launch (pbr_cartpole_step)
 
     # Rendering defaults
     num_channels: int = 3

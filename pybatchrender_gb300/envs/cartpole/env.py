@@ -1,6 +1,13 @@
 """CartPole environment (``envs/cartpole/env.py``): Euler-integrated
 dynamics, termination, survival reward and auto-reset, all on the env's
-device; pixels come from ``render_pixels`` each step."""
+device; pixels come from ``render_pixels`` each step.
+
+On a CUDA device the step's arithmetic is one fused launch
+(``pbr_cartpole_step``) instead of about forty elementwise tensor operations;
+it follows those operations rounding by rounding, and the initial states of
+the auto-reset are drawn by the same tensor RNG calls in the same order.
+``fused_step=False`` keeps the tensor-operation step."""
+import ctypes
 import math
 
 import torch
@@ -28,6 +35,9 @@ class CartPoleEnv(PBREnv):
         self.x_threshold = float(cfg.x_threshold)
         self.max_steps = int(cfg.max_steps)
         self.auto_reset = bool(cfg.auto_reset)
+        self.fused_step = bool(getattr(cfg, "fused_step", True))
+        self._consts = (ctypes.c_double * 9)(self.gravity, self.masscart, self.masspole, self.length, self.force_mag,
+                                             self.tau, self.x_threshold, self.theta_threshold, self.max_steps)
         self.seed = int(cfg.seed)
         self.render = bool(cfg.render)
         th0_lo, th0_hi = float(cfg.init_theta_range_deg[0]), float(cfg.init_theta_range_deg[1])
@@ -39,11 +49,14 @@ class CartPoleEnv(PBREnv):
         if self.seed is not None:
             self.set_seed(self.seed)
 
-    def _sample_initial_state(self, batch_shape: torch.Size) -> torch.Tensor:
+    def _sample_initial_columns(self, batch_shape: torch.Size) -> list[torch.Tensor]:
         def u(lo_hi):
             return torch.empty(*batch_shape, 1, dtype=torch.float32, device=self.device).uniform_(*lo_hi)
-        return torch.cat([u(self.cfg.init_x_range), u(self.cfg.init_x_dot_range), u(self._init_theta_range_rad),
-                          u(self._init_theta_dot_range_rad)], dim=-1)
+        return [u(self.cfg.init_x_range), u(self.cfg.init_x_dot_range), u(self._init_theta_range_rad),
+                u(self._init_theta_dot_range_rad)]
+
+    def _sample_initial_state(self, batch_shape: torch.Size) -> torch.Tensor:
+        return torch.cat(self._sample_initial_columns(batch_shape), dim=-1)
 
     def _dynamics(self, obs: torch.Tensor, action: torch.Tensor) -> torch.Tensor:
         """``envs/cartpole/env.py:111-129``."""
@@ -93,6 +106,8 @@ class CartPoleEnv(PBREnv):
             if step_count is None:
                 step_count = torch.zeros_like(obs[..., 0], dtype=torch.long, device=self.device)
         action = tensordict["action"].to(self.device)
+        if self.fused_step and obs.is_cuda:
+            return self._fused_step(obs, action, step_count)
         next_obs_raw = self._dynamics(obs, action)
         done = self._termination(next_obs_raw, step_count)
         reward = self._reward(next_obs_raw, done)
@@ -106,4 +121,33 @@ class CartPoleEnv(PBREnv):
         out = {"observation": next_obs, "reward": reward, "done": done, "step_count": next_step_count}
         if pixels is not None:
             out["pixels"] = pixels
+        return TensorDict(out, batch_size=self.batch_size)
+
+    def _fused_step(self, obs: torch.Tensor, action: torch.Tensor, step_count: torch.Tensor):
+        """The step above as one ``pbr_cartpole_step`` launch (graph-capturable:
+        no host synchronisation, outputs from the caching allocator)."""
+        from ... import _capi
+        lib = _capi.load()
+        obs = obs.to(torch.float32).contiguous()
+        bs = obs.shape[:-1]
+        n = obs.numel() // 4
+        act = action.reshape(bs).to(torch.int64).contiguous()
+        sc = step_count.reshape(bs).to(torch.int64).contiguous()
+        resets = [None] * 4
+        if self.auto_reset:
+            resets = self._sample_initial_columns(bs)  # the tensor path's RNG calls, in its order
+        raw = torch.empty_like(obs)
+        nxt = torch.empty_like(obs)
+        reward = torch.empty(*bs, 1, dtype=torch.float32, device=obs.device)
+        done = torch.empty(*bs, 1, dtype=torch.bool, device=obs.device)
+        nsc = torch.empty(*bs, dtype=torch.int64, device=obs.device)
+        stream = torch.cuda.current_stream(obs.device).cuda_stream
+        rc = lib.pbr_cartpole_step(_capi.ptr(obs), _capi.ptr(act), _capi.ptr(sc), *[_capi.ptr(t) for t in resets],
+                                   _capi.ptr(raw), _capi.ptr(nxt), _capi.ptr(reward), _capi.ptr(done), _capi.ptr(nsc),
+                                   n, self._consts, int(self.auto_reset), ctypes.c_void_p(stream))
+        if rc != 0:
+            raise _capi.PBRError("pbr_cartpole_step", rc, "invalid arguments or launch failure")
+        out = {"observation": nxt, "reward": reward, "done": done, "step_count": nsc}
+        if self.render:
+            out["pixels"] = self.render_pixels(raw)
         return TensorDict(out, batch_size=self.batch_size)

@@ -73,6 +73,12 @@ int pbr_destroy(pbr_ctx* ctx);
 int pbr_mesh_register(pbr_ctx* ctx, const float* d_pos, const float* d_nrm, const int32_t* d_idx,
                       int nv, int nt, int smooth, int* out_mesh_id);
 
+/* Bounding sphere of a registered mesh (centre and radius in mesh
+ * coordinates, every vertex within it).  With it the tile kernel skips the
+ * instances whose bound projects outside the pixel region it is drawing.
+ * Optional (radius 0: no skipping); no counterpart in the reference. */
+int pbr_mesh_set_bounds(pbr_ctx* ctx, int mesh_id, float cx, float cy, float cz, float radius);
+
 /* Attach texture coordinates to a registered mesh: d_uv [nv,2] float32
  * (GL convention, v = 0 at the bottom of the image), or NULL for none (all
  * coordinates 0).  Replaces the p3d_MultiTexCoord0 vertex column that

@@ -34,6 +34,7 @@ SIGNATURES: dict[str, list] = {
     "pbr_create": [ctypes.POINTER(_vp), _i, _i, _i, _i, _i],
     "pbr_destroy": [_vp],
     "pbr_mesh_register": [_vp, _vp, _vp, _vp, _i, _i, _i, _pi],
+    "pbr_mesh_set_bounds": [_vp, _i, _f, _f, _f, _f],
     "pbr_mesh_set_uv": [_vp, _i, _vp],
     "pbr_node_add": [_vp, _i, _i, _i, _pi],
     "pbr_node_set_texture": [_vp, _i, _vp, _i, _i],

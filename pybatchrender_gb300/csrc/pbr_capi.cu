@@ -362,6 +362,15 @@ int pbr_mesh_register(pbr_ctx* ctx, const float* d_pos, const float* d_nrm, cons
   return PBR_OK;
 }
 
+int pbr_mesh_set_bounds(pbr_ctx* ctx, int mesh_id, float cx, float cy, float cz, float radius) {
+  PBR_CHECK_CTX(ctx);
+  if (mesh_id < 0 || mesh_id >= ctx->P.num_meshes) return set_err(ctx, PBR_ERR_INVALID, "unknown mesh id %d", mesh_id);
+  if (!(radius >= 0.f) || !std::isfinite(cx) || !std::isfinite(cy) || !std::isfinite(cz) || !std::isfinite(radius))
+    return set_err(ctx, PBR_ERR_INVALID, "mesh bounds must be finite with radius >= 0");
+  ctx->P.meshes[mesh_id].bound = make_float4(cx, cy, cz, radius);
+  return PBR_OK;
+}
+
 int pbr_mesh_set_uv(pbr_ctx* ctx, int mesh_id, const float* d_uv) {
   PBR_CHECK_CTX(ctx);
   if (mesh_id < 0 || mesh_id >= ctx->P.num_meshes) return set_err(ctx, PBR_ERR_INVALID, "unknown mesh id %d", mesh_id);

@@ -34,6 +34,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
   int* s_scan = reinterpret_cast<int*>(smem + L.misc);
   float* s_vp = reinterpret_cast<float*>(s_scan + 2 * NW + 8);
   int* s_item = reinterpret_cast<int*>(s_vp + 16);
+  uint32_t* s_keep = reinterpret_cast<uint32_t*>(s_item + 4);           // [kInstWords] kept instances of a batch
+  int* s_ci = reinterpret_cast<int*>(s_keep + kInstWords);              // [kMaxInstBatch] their batch indices
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = P.W, H = P.H;
@@ -302,7 +304,69 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           icache[i * 4 + 3] = make_float4(cc[0], cc[1], cc[2], cc[3]);
         }
         __syncthreads();
-        const int total_t = nbc * nt;
+        // Instances whose bounding sphere projects entirely above or below this region's rows,
+        // or left or right of the image, cannot cover a pixel centre here: the batch is
+        // compacted to the others, in draw order.  The projection of the sphere's world-space
+        // box (eight corners, all in front of the camera, else the instance is kept) bounds the
+        // projection of the mesh.
+        const bool can_cull = me.bound.w > 0.f;
+        int nb = nbc;
+        if (can_cull) {
+          for (int i0c = 0; i0c < nbc; i0c += THREADS) {
+            const int i = i0c + tid;
+            bool keep = false;
+            if (i < nbc) {
+              const float4 r0 = icache[i * 4 + 0], r1 = icache[i * 4 + 1], r2 = icache[i * 4 + 2];
+              const float4 b = me.bound;
+              const float wx = r0.x * b.x + r0.y * b.y + r0.z * b.z + r0.w;
+              const float wy = r1.x * b.x + r1.y * b.y + r1.z * b.z + r1.w;
+              const float wz = r2.x * b.x + r2.y * b.y + r2.z * b.z + r2.w;
+              // world radius: mesh radius times the largest column norm of the linear part
+              const float n0 = r0.x * r0.x + r1.x * r1.x + r2.x * r2.x;
+              const float n1 = r0.y * r0.y + r1.y * r1.y + r2.y * r2.y;
+              const float n2 = r0.z * r0.z + r1.z * r1.z + r2.z * r2.z;
+              const float R = b.w * sqrtf(fmaxf(fmaxf(n0, n1), n2)) * 1.0001f + 1e-6f;
+              const float cx = vp0 * wx + vp1 * wy + vp2 * wz + vp3, cy = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
+              const float cw = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
+              float xmin = 3.0e38f, xmax = -3.0e38f, ymin = 3.0e38f, ymax = -3.0e38f;
+              bool front = true;
+#pragma unroll
+              for (int corner = 0; corner < 8; ++corner) {
+                const float sx = (corner & 1) ? R : -R, sy = (corner & 2) ? R : -R, sz = (corner & 4) ? R : -R;
+                const float x = cx + vp0 * sx + vp1 * sy + vp2 * sz;
+                const float y = cy + vp4 * sx + vp5 * sy + vp6 * sz;
+                const float w = cw + vp12 * sx + vp13 * sy + vp14 * sz;
+                front = front && (w > 1e-6f);
+                const float iw = 1.f / w;
+                const float px = (x * iw + 1.f) * 0.5f * S.W, py = (1.f - y * iw) * 0.5f * S.H;
+                xmin = fminf(xmin, px);
+                xmax = fmaxf(xmax, px);
+                ymin = fminf(ymin, py);
+                ymax = fmaxf(ymax, py);
+              }
+              // two pixels of slack; a NaN anywhere keeps the instance (every comparison is false)
+              const bool out = front && (ymax < S.ry0 - 2.f || ymin > S.ry1 + 3.f || xmax < -2.f || xmin > S.W + 2.f);
+              keep = !out;
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0 && i0c + warp * 32 < kMaxInstBatch) s_keep[(i0c >> 5) + warp] = bal;
+          }
+          __syncthreads();
+          int total_keep = 0;
+          const int words_b = (nbc + 31) >> 5;
+          for (int wd = 0; wd < words_b; ++wd) total_keep += __popc(s_keep[wd]);
+          for (int i = tid; i < nbc; i += THREADS) {
+            const uint32_t word = s_keep[i >> 5];
+            if ((word >> (i & 31)) & 1u) {
+              int slot = __popc(word & ((1u << (i & 31)) - 1u));
+              for (int wd = 0; wd < (i >> 5); ++wd) slot += __popc(s_keep[wd]);
+              s_ci[slot] = i;
+            }
+          }
+          nb = total_keep;
+          __syncthreads();
+        }
+        const int total_t = nb * nt;
         for (int t0 = 0; t0 < total_t; t0 += RT) {
           // up to 2 emitted triangles per source triangle (near-plane clip)
           const int rem = min(RT, total_t - t0);
@@ -315,6 +379,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             const int t = t0 + tid;
             li = t / nt;
             ti = t - li * nt;
+            if (can_cull) li = s_ci[li];
             i0 = me.idx[3 * ti];
             i1 = me.idx[3 * ti + 1];
             i2 = me.idx[3 * ti + 2];

@@ -15,6 +15,8 @@ namespace pbr {
 constexpr int kMaxNodes = 24;
 constexpr int kMaxMeshes = 24;
 constexpr int kPx = 16;  // pixels per thread: one 128-bit store per channel
+constexpr int kMaxInstBatch = 256;               // instances per batch of the tile kernel (icap)
+constexpr int kInstWords = kMaxInstBatch / 32;
 
 enum : int { kModeHpr = 0, kModeRot = 1, kModeMat = 2 };
 
@@ -30,6 +32,7 @@ struct MeshDesc {
   const int32_t* idx;  // [nt,3]
   const float* uv;     // [nv,2] texture coordinates, or null (all 0)
   int32_t nv, nt, smooth, pad;
+  float4 bound;        // bounding sphere (centre, radius) in mesh coordinates; radius <= 0: unknown
 };
 
 struct NodeDesc {
@@ -119,7 +122,7 @@ struct SmemLayout {
   int vcache;              // float4 [vcap*2]: clip position, world normal
   int icache;              // float4 [icap*4]: model matrix rows, colour
   int state;               // per-pixel depth / emit-order keys of the region [threads*kPx] (uint64)
-  int misc;                // per-warp survivor counts (two rounds), VP, work item
+  int misc;                // per-warp survivor counts (two rounds), VP, work item, instance compaction
   int total;
 };
 
@@ -153,7 +156,7 @@ __host__ __device__ inline SmemLayout smem_layout(const RasterArgs& a, int threa
   L.icache = off; off += align16(a.icap * 64);
   L.state = off;  // depth / emit-order keys of the region's pixels, uint64 each
   off += align16(threads * kPx * 8);
-  L.misc = off; off += align16((2 * (threads / 32) + 8) * 4 + 16 * 4 + 16);
+  L.misc = off; off += align16((2 * (threads / 32) + 8) * 4 + 16 * 4 + 16 + (kInstWords + kMaxInstBatch) * 4);
   L.total = off;
   return L;
 }

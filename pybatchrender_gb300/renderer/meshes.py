@@ -70,6 +70,16 @@ class Mesh:
     def tight_bounds(self) -> tuple[np.ndarray, np.ndarray]:
         return self.positions.min(axis=0), self.positions.max(axis=0)
 
+    def bounding_sphere(self) -> tuple[tuple[float, float, float], float]:
+        """(centre, radius) containing every vertex: the bounds-box centre and
+        the largest distance to it, widened by a relative 1e-5."""
+        if self.positions.size == 0:
+            return (0.0, 0.0, 0.0), 0.0
+        p = self.positions.astype(np.float64)
+        c = (p.min(axis=0) + p.max(axis=0)) * 0.5
+        r = float(np.sqrt(((p - c) ** 2).sum(axis=1)).max())
+        return (float(c[0]), float(c[1]), float(c[2])), r * (1.0 + 1e-5) + 1e-7
+
     def copy(self) -> "Mesh":
         return Mesh(self.positions.copy(), self.normals.copy(), self.indices.copy(), self.name,
                     uvs=None if self.uvs is None else self.uvs.copy(), texture=self.texture)

@@ -491,6 +491,8 @@ class PBRRenderer:
                     mid = ctypes.c_int()
                     _capi.call(lib, ctx, "pbr_mesh_register", _capi.ptr(pos), _capi.ptr(nrm), _capi.ptr(idx),
                                m.num_vertices, m.num_triangles, int(m.smooth), ctypes.byref(mid))
+                    c, rad = m.bounding_sphere()
+                    _capi.call(lib, ctx, "pbr_mesh_set_bounds", mid.value, *c, rad)
                     if m.uvs is not None:
                         uv = torch.from_numpy(m.uvs).to(self.device)
                         self._mesh_tensors.append((uv,))

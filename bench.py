@@ -43,6 +43,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -95,7 +96,7 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{index}.csv")
+        self.path = os.path.join(os.environ.get("PBR_CLOCKS_DIR", tempfile.gettempdir()), f"clocks_gpu{index}.csv")
 
     def __enter__(self):
         try:

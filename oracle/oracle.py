@@ -1,7 +1,7 @@
 """Python side of the oracle: ctypes bindings to ``liboracle.so`` (built from
 ``raster_ref.c``) plus helpers to build, render and compare.
 
-TEST INFRASTRUCTURE ONLY.  The oracle is the checker for the CUDA renderer
+TEST INFRASTRUCTURE ONLY.  The oracle is the parity reference for the CUDA renderer
 and the timed CPU baseline; the product package never imports this module.
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its
 ``cpu_baseline`` leg and ``--impl reference`` arm) may use it.

@@ -7,7 +7,7 @@
  * "--impl reference" arm) use it.
  *
  * Built twice from this one source (see oracle/Makefile / oracle/build.py):
- *   REAL=double  -> symbols *_f64  (the FP64 checker)
+ *   REAL=double  -> symbols *_f64  (the FP64 parity reference)
  *   REAL=float   -> symbols *_f32  (the FP32 multithreaded CPU baseline)
  *
  * What it restates (paths relative to the reference project):

@@ -1,6 +1,6 @@
 """Dense float64 PyTorch restatement of the soft-coverage model.
 
-TEST INFRASTRUCTURE ONLY (the checker for the CUDA soft forward and adjoint).
+TEST INFRASTRUCTURE ONLY (a parity reference for the CUDA soft forward and adjoint).
 Every pixel is evaluated against every triangle (no binning), in float64, and
 torch autograd gives the reference gradients.  The model is the one of
 ``oracle/raster_ref.c`` (``orc_render_soft``): vertex transform of

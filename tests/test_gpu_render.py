@@ -1,7 +1,7 @@
 """Hard-raster parity: the CUDA renderer (through the C ABI) against the FP64
 oracle (oracle/raster_ref.c) on the same seeded scenes.
 
-Bar (the benchmark spec): winner (which triangle covers the pixel, i.e. coverage and
+Bar: winner (which triangle covers the pixel, i.e. coverage and
 depth order) identical to the oracle except at pixels the oracle flags as
 ambiguous (centre within 1e-4 px of an edge of a visible triangle, or two
 fragments within 2e-6 in window depth); colour within 1/255 per channel on

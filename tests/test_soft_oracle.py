@@ -1,4 +1,4 @@
-"""Soft-coverage checker consistency (CPU): the FP64 C oracle, the dense
+"""Soft-coverage reference consistency (CPU): the FP64 C oracle, the dense
 float64 PyTorch reference and FP64 finite differences describe one model."""
 import numpy as np
 import torch

@@ -185,3 +185,19 @@ def test_steering_env_dynamics_cpu():
     assert (nxt["reward"] == 0.0).all()
     a = env.action_spec.rand()
     assert a.shape == (4, 1) and (a.abs() <= 327.68).all()
+
+
+def test_template_env_runs_cpu():
+    """The template environment works as shipped (no pixels on the CPU)."""
+    from pybatchrender_gb300.envs._template import MyEnv, MyEnvConfig, MyEnvRenderer
+    envs.register("Template-v0", MyEnv, MyEnvRenderer, MyEnvConfig)
+    try:
+        env = envs.make("Template-v0", num_scenes=6, device="cpu", render=False, max_steps=5)
+        td = env.reset()
+        for _ in range(6):
+            td["action"] = env.action_spec.rand()
+            td = env.step(td)["next"]
+        assert td["observation"].shape == (6, 2) and td["reward"].shape == (6, 1)
+        assert int(td["step_count"].max()) < 5  # max_steps reached once: every scene was reset
+    finally:
+        envs.unregister("Template-v0")

@@ -97,3 +97,18 @@ def test_fused_step_in_graph_with_render(cuda):
         ref = env._renderer.step(raw)
         assert torch.equal(o["pixels"], ref)
         obs, sc = o["observation"].clone(), o["step_count"].clone()
+
+
+def test_template_env_renders(cuda, oracle):
+    """The template environment on the GPU: state-bound render, parity with the
+    oracle, and the box follows the state."""
+    from pybatchrender_gb300.envs._template import MyEnv, MyEnvConfig, MyEnvRenderer
+    from tests.test_gpu_render import check_parity
+    cfg = MyEnvConfig(num_scenes=32, device="cuda")
+    env = MyEnv(MyEnvRenderer(cfg), cfg)
+    td = env.reset()
+    assert td["pixels"].shape == (32, 3, 64, 64)
+    td["action"] = torch.ones(32, dtype=torch.long, device="cuda")
+    nxt = env.step(td)["next"]
+    assert not torch.equal(nxt["pixels"], td["pixels"])
+    check_parity(env._renderer, oracle)

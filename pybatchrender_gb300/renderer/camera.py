@@ -243,6 +243,13 @@ class PBRCam(PBRShaderContext):
         if not lazy:
             self._update_vp()
 
+    def start_tasks(self, taskMgr=None, name: str = "pbr_cam_update") -> None:
+        """``camera.py:404-420`` registers a per-frame task that re-uploads the
+        view-projection and the screen size.  Here every setter writes
+        ``VP_k44`` in place, which the kernels read at each launch, and there is
+        no Panda3D base camera to follow: nothing to schedule."""
+        return None
+
     def get_eye(self) -> torch.Tensor:
         return self.eye_k3.clone()
 

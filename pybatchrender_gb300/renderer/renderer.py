@@ -64,6 +64,11 @@ class PBRRenderer:
         self._plain_staging: dict = {}
         self.autotune_result = None
         self._state_bindings: list[tuple[PBRNode, int, int]] = []
+        # keyboard state of the manual camera control (renderer.py:162-222); no window here, so the keys are
+        # set through set_key and update_camera applies them
+        self.keys = {"w": False, "s": False, "a": False, "d": False, "z": False, "x": False}
+        self._camera_speed = 25.0
+        self._last_camera_update: float | None = None
 
     # ------------------------------------------------------------- scene API
     def set_background_color(self, r: float, g: float, b: float, a: float = 1.0) -> None:
@@ -108,6 +113,37 @@ class PBRRenderer:
         self._graph = None
         if self._ctx is not None:
             self._build_context()
+
+    # ------------------------------------------------------ manual camera control
+    def set_key(self, key, value) -> None:
+        """``renderer.py:162-163``."""
+        self.keys[key] = value
+
+    def enable_camera_control(self) -> None:
+        """``renderer.py:165-197``: there is no window to take keyboard and mouse
+        input from, which is the reference's offscreen case: warn and switch
+        the option off."""
+        print('WARNING: Manual camera control is not possible in offscreen mode, disabling.')
+        self.cfg.manual_camera_control = False
+
+    def update_camera(self, task=None, dt: float | None = None):
+        """Keyboard part of ``renderer.py:199-222``: move every scene's eye by
+        ``25 * dt`` along +y (w), -y (s), -x (a), +x (d), +z (z), -z (x).  ``dt``
+        defaults to the time since the previous call.  There is no mouse."""
+        import time
+        now = time.perf_counter()
+        if dt is None:
+            dt = 0.0 if self._last_camera_update is None else now - self._last_camera_update
+        self._last_camera_update = now
+        if self._pbr_cam is not None:
+            eye = self._pbr_cam.get_eye().reshape(-1, 3).clone()
+            step = self._camera_speed * float(dt)
+            for key, axis, sign in (("w", 1, 1.0), ("s", 1, -1.0), ("a", 0, -1.0), ("d", 0, 1.0), ("z", 2, 1.0),
+                                    ("x", 2, -1.0)):
+                if self.keys.get(key):
+                    eye[:, axis] += sign * step
+            self._pbr_cam.set_eye(eye)
+        return getattr(task, "cont", None)
 
     def add_camera(self, fov_y_deg: float = 55.0, z_near: float = 0.05, z_far: float = 100.0,
                    fixed_projection: bool = True) -> PBRCam:

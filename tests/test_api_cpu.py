@@ -201,3 +201,16 @@ def test_template_env_runs_cpu():
         assert int(td["step_count"].max()) < 5  # max_steps reached once: every scene was reset
     finally:
         envs.unregister("Template-v0")
+
+
+def test_manual_camera_control_headless():
+    r = pbr.PBRRenderer(num_scenes=2, device="cpu")
+    cam = r.add_camera()
+    r.enable_camera_control()  # no window: warns and switches the option off
+    assert r.cfg.manual_camera_control is False
+    eye0 = cam.get_eye().reshape(-1, 3).clone()
+    r.set_key("w", True)
+    r.set_key("a", True)
+    r.update_camera(dt=0.1)
+    eye1 = cam.get_eye().reshape(-1, 3)
+    assert torch.allclose(eye1 - eye0, torch.tensor([[-2.5, 2.5, 0.0]]).expand(2, 3))

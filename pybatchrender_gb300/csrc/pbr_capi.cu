@@ -42,7 +42,7 @@ struct pbr_ctx {
   uint32_t* d_cbuf = nullptr;
   // cudaFuncSetAttribute cache: [threads idx][plain][winner]
   int smem_set[3][2][2][2] = {};
-  int small_smem_set[2][2][2] = {};
+  int small_smem_set[2][2][3] = {};
   int soft_small_smem_set[2] = {};
   int soft_large_smem_set[2] = {};
   float4* d_soft_scratch = nullptr;  // binned soft kernel slabs, grown on demand
@@ -214,7 +214,7 @@ static int plan_small(pbr_ctx* ctx, bool plain, bool winner, int n0, int n1, Lau
     insts += nd.ips;
     verts += (long long)nd.ips * me.nv;
     if (me.smooth) A.smooth_any = 1;
-    if (nd.tex) return set_err(ctx, PBR_ERR_CAPACITY, "textured nodes are drawn by the tile kernel");
+    if (nd.tex) A.smooth_any = A.tex_any = 1;  // textured triangles are shaded per pixel
   }
   if (insts > 32 || verts > 256)
     return set_err(ctx, PBR_ERR_CAPACITY, "scene too large for the scene-per-warp kernel");
@@ -226,9 +226,10 @@ static int plan_small(pbr_ctx* ctx, bool plain, bool winner, int n0, int n1, Lau
   if (per_warp < 0) return set_err(ctx, PBR_ERR_CAPACITY, "image too large for the scene-per-warp kernel");
   const int smem = per_warp * warps;
   if (smem > ctx->max_smem) return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp layout exceeds shared memory");
-  int& cached = ctx->small_smem_set[plain ? 1 : 0][winner ? 1 : 0][A.smooth_any ? 1 : 0];
+  const int shade = A.tex_any ? 2 : (A.smooth_any ? 1 : 0);
+  int& cached = ctx->small_smem_set[plain ? 1 : 0][winner ? 1 : 0][shade];
   if (smem > 48 * 1024 && smem > cached) {
-    cudaError_t e = pbr::small_set_smem_limit(plain, winner, A.smooth_any != 0, smem);
+    cudaError_t e = pbr::small_set_smem_limit(plain, winner, shade, smem);
     if (e != cudaSuccess) return cuda_err(ctx, e, "cudaFuncSetAttribute");
     cached = smem;
   }

@@ -19,8 +19,8 @@ cudaError_t hard_launch(int threads, bool plain, bool winner, const SceneParams&
 // Scene-per-warp raster (pbr_small.cu); blocks of small_warps() warps.
 int small_warps();
 int small_smem_per_warp(const RasterArgs& A, int W, int H);  // -1: image has more than 64 bins
-cudaError_t small_set_smem_limit(bool plain, bool winner, bool smooth, int bytes);
-cudaError_t small_occupancy(bool plain, bool winner, bool smooth, int smem_bytes, int* blocks_per_sm);
+cudaError_t small_set_smem_limit(bool plain, bool winner, int shade, int bytes);  // shade 0 flat, 1 smooth, 2 textured
+cudaError_t small_occupancy(bool plain, bool winner, int shade, int smem_bytes, int* blocks_per_sm);
 cudaError_t small_launch(bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int grid, int smem_bytes,
                          cudaStream_t stream);
 // Soft coverage (pbr_soft.cu); threads in {128, 256}.

@@ -43,21 +43,22 @@ constexpr int kWarps = 4;   // warps per block
 constexpr int kBlocksPerSm = 7;
 
 struct SmallLayout {
-  int t0, t1, t2, t3, bgrec, t4, s0, s1, s2, s3, masks, vp, uni;
+  int t0, t1, t2, t3, bgrec, t4, s0, s1, s2, s3, s4, s5, masks, vp, uni;
   int vcache, itab;  // inside uni (setup)
   int keys;          // inside uni (raster): uint64 [16][32]
   int per_warp;
 };
 
-// Per-warp shared memory.  Triangle records T0..T4 (and S0..S3 for smooth
-// shading; textured scenes take the tile kernel); bgrec is a T4-shaped record just before T4[0] holding the
+// Per-warp shared memory.  Triangle records T0..T4 (S0..S3 for per-pixel
+// shading, S4..S5 for texture coordinates); bgrec is a T4-shaped record just before T4[0] holding the
 // background colour (.z) and winner -1 (.w), so that draw order + 1 indexes
 // both.  The setup stage's vertex cache (3 float4 per vertex: clip position;
 // normal with .w = z + w; screen position), instance table (5 float4 per
 // instance: 3 model-matrix rows, colour, meta) and view-projection matrix
 // share one region with the raster stage's key tile.  Cartpole-sized scenes
 // need 8064 bytes a warp, which keeps 7 blocks of 4 warps on an SM.
-__host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int icap, int nbins, int smooth) {
+__host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int icap, int nbins, int smooth,
+                                                    int tex) {
   SmallLayout L;
   int off = 0;
   const int t4 = tri_cap * 16;
@@ -75,6 +76,12 @@ __host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int i
   } else {
     L.s0 = L.s1 = L.s2 = L.s3 = 0;
   }
+  if (smooth && tex) {
+    L.s4 = off; off += align16(t4);
+    L.s5 = off; off += align16(t4);
+  } else {
+    L.s4 = L.s5 = 0;
+  }
   L.masks = off; off += align16(nbins * ((tri_cap + 31) / 32) * 4);
   L.uni = off;
   const int setup = align16(vcap * 48) + align16(icap * 80) + 64;
@@ -91,7 +98,7 @@ __host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int i
 int small_smem_per_warp(const RasterArgs& A, int W, int H) {
   const int nbins = ((W + kBinW - 1) / kBinW) * ((H + kBinH - 1) / kBinH);
   if (nbins > 64) return -1;  // the non-empty bins of a scene are one 64-bit mask
-  return small_layout(A.tri_cap, A.vcap, A.icap, nbins, A.smooth_any).per_warp;
+  return small_layout(A.tri_cap, A.vcap, A.icap, nbins, A.smooth_any, A.tex_any).per_warp;
 }
 
 // RGBA words of pixels p0..p3 -> channel-planar words (4 pixels per word).
@@ -114,7 +121,7 @@ __device__ __forceinline__ int node_count(const NodeDesc& nd, int k) {
 // Smooth meshes take the vertex normals from the vertex cache; a flat mesh's
 // triangle is lit with its first vertex's normal (all three are identical),
 // transformed here, only for triangles that survive culling.
-template <bool WRITE, bool SMOOTH>
+template <bool WRITE, bool SMOOTH, bool TEX>
 __device__ __forceinline__ int small_tri(const SceneParams& P, const SetupCtx& S, const float4* vcache,
                                          const float4* itab, int total_inst, int t, int slot) {
   int inst = 0;
@@ -129,7 +136,16 @@ __device__ __forceinline__ int small_tri(const SceneParams& P, const SetupCtx& S
   if (!front && n0.w < 0.f && n1.w < 0.f && n2.w < 0.f) return 0;
   const float4 col = itab[inst * 5 + 3];
   const int draw_id = __float_as_int(meta.z) + ti;
-  const bool smooth = SMOOTH && me.smooth != 0;
+  const int node = __float_as_int(meta.x);
+  const bool textured = TEX && P.nodes[node].tex != nullptr;  // shaded per pixel like smooth meshes
+  const bool smooth = SMOOTH && (me.smooth != 0 || textured);
+  TexIn tx;
+  if (WRITE && textured) {
+    tx.t0 = mesh_uv(me, i0);
+    tx.t1 = mesh_uv(me, i1);
+    tx.t2 = mesh_uv(me, i2);
+    tx.node = node;
+  }
   if (WRITE && !SMOOTH) {
     const float4 r0 = itab[inst * 5 + 0], r1 = itab[inst * 5 + 1], r2 = itab[inst * 5 + 2];
     const float ax = me.nrm[3 * i0], ay = me.nrm[3 * i0 + 1], az = me.nrm[3 * i0 + 2];
@@ -145,22 +161,24 @@ __device__ __forceinline__ int small_tri(const SceneParams& P, const SetupCtx& S
   if (front) {
     const float4 a = vcache[3 * (vbase + i0) + 2], b = vcache[3 * (vbase + i1) + 2], c = vcache[3 * (vbase + i2) + 2];
     return setup_tri_sv<WRITE>(P, S, SV{a.x, a.y, a.z, a.w}, n0, SV{b.x, b.y, b.z, b.w}, n1, SV{c.x, c.y, c.z, c.w},
-                               n2, slot, col, draw_id, smooth);
+                               n2, slot, col, draw_id, smooth, tx);
   }
   return clip_tri<WRITE>(P, S, vcache[3 * (vbase + i0)], n0, vcache[3 * (vbase + i1)], n1, vcache[3 * (vbase + i2)],
-                         n2, i0, i1, i2, slot, col, draw_id, smooth);
+                         n2, i0, i1, i2, slot, col, draw_id, smooth, tx);
 }
 
-template <bool PLAIN, bool WINNER, bool SMOOTH>
+// SHADE: 0 = flat meshes only, 1 = smooth meshes (per-pixel normals), 2 = smooth and textured
+template <bool PLAIN, bool WINNER, int SHADE>
 __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const __grid_constant__ SceneParams P,
                                                                          const __grid_constant__ RasterArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
+  constexpr bool SMOOTH = SHADE >= 1, TEX = SHADE == 2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int W = P.W, H = P.H, HW = W * H, C = P.C;
   const int bins_x = (W + kBinW - 1) / kBinW, bins_y = (H + kBinH - 1) / kBinH;
   const int nbins = bins_x * bins_y;
   const int words = (A.tri_cap + 31) >> 5;
-  const SmallLayout L = small_layout(A.tri_cap, A.vcap, A.icap, nbins, SMOOTH ? 1 : 0);
+  const SmallLayout L = small_layout(A.tri_cap, A.vcap, A.icap, nbins, SMOOTH ? 1 : 0, TEX ? 1 : 0);
   unsigned char* base = smem + warp * L.per_warp;
   SetupCtx S;
   S.T0 = reinterpret_cast<float4*>(base + L.t0);
@@ -172,7 +190,8 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
   S.S1 = reinterpret_cast<float4*>(base + L.s1);
   S.S2 = reinterpret_cast<float4*>(base + L.s2);
   S.S3 = reinterpret_cast<float4*>(base + L.s3);
-  S.S4 = S.S5 = nullptr;  // no textured triangles in this kernel
+  S.S4 = reinterpret_cast<float4*>(base + L.s4);
+  S.S5 = reinterpret_cast<float4*>(base + L.s5);
   S.W = (float)W;
   S.H = (float)H;
   S.ry0 = 0.f;
@@ -279,7 +298,7 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
     int tri_count = 0;
     for (int t0 = 0; t0 < total_tris; t0 += 32) {
       const int t = t0 + lane;
-      const int c = t < total_tris ? small_tri<false, SMOOTH>(P, S, vcache, itab, total_inst, t, 0) : 0;
+      const int c = t < total_tris ? small_tri<false, SMOOTH, TEX>(P, S, vcache, itab, total_inst, t, 0) : 0;
       int incl = c;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -287,7 +306,7 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
         if (lane >= o) incl += y;
       }
       const int total = __shfl_sync(0xffffffffu, incl, 31);
-      if (c > 0) small_tri<true, SMOOTH>(P, S, vcache, itab, total_inst, t, tri_count + incl - c);
+      if (c > 0) small_tri<true, SMOOTH, TEX>(P, S, vcache, itab, total_inst, t, tri_count + incl - c);
       tri_count += total;
     }
     __syncwarp();
@@ -451,7 +470,7 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
               if (PLAIN && r == 0) {
                 col[q] = A.cbuf[lane_pix + boff + j];
               } else if (SMOOTH && (__float_as_uint(rec->y) & 8u)) {
-                col[q] = shade_smooth<false>(P, S, (int)r - 1, (float)(col0 + seg_x + j) + 0.5f, (float)(row0 + seg_r) + 0.5f);
+                col[q] = shade_smooth<TEX>(P, S, (int)r - 1, (float)(col0 + seg_x + j) + 0.5f, (float)(row0 + seg_r) + 0.5f);
               } else {
                 col[q] = __float_as_uint(rec->z);
               }
@@ -500,34 +519,46 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
 
 // ---------------------------------------------------------------------------
 
-template <bool PL, bool WN, bool SM>
+template <bool PL, bool WN, int SH>
 static const void* small_fn() {
-  return reinterpret_cast<const void*>(&small_kernel<PL, WN, SM>);
+  return reinterpret_cast<const void*>(&small_kernel<PL, WN, SH>);
 }
 
-static const void* pick_small(bool plain, bool winner, bool smooth) {
-  if (plain && winner) return nullptr;
-  if (smooth) return plain ? small_fn<true, false, true>() : (winner ? small_fn<false, true, true>() : small_fn<false, false, true>());
-  return plain ? small_fn<true, false, false>() : (winner ? small_fn<false, true, false>() : small_fn<false, false, false>());
+template <int SH>
+static const void* pick_shade(bool plain, bool winner) {
+  return plain ? small_fn<true, false, SH>() : (winner ? small_fn<false, true, SH>() : small_fn<false, false, SH>());
 }
+
+// shade: 0 = flat meshes only, 1 = smooth meshes, 2 = textured nodes (per-pixel shading)
+static const void* pick_small(bool plain, bool winner, int shade) {
+  if (plain && winner) return nullptr;
+  switch (shade) {
+    case 0: return pick_shade<0>(plain, winner);
+    case 1: return pick_shade<1>(plain, winner);
+    case 2: return pick_shade<2>(plain, winner);
+  }
+  return nullptr;
+}
+
+static int shade_of(const RasterArgs& A) { return A.tex_any ? 2 : (A.smooth_any ? 1 : 0); }
 
 int small_warps() { return kWarps; }
 
-cudaError_t small_set_smem_limit(bool plain, bool winner, bool smooth, int bytes) {
-  const void* f = pick_small(plain, winner, smooth);
+cudaError_t small_set_smem_limit(bool plain, bool winner, int shade, int bytes) {
+  const void* f = pick_small(plain, winner, shade);
   if (!f) return cudaErrorInvalidValue;
   return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-cudaError_t small_occupancy(bool plain, bool winner, bool smooth, int smem_bytes, int* blocks_per_sm) {
-  const void* f = pick_small(plain, winner, smooth);
+cudaError_t small_occupancy(bool plain, bool winner, int shade, int smem_bytes, int* blocks_per_sm) {
+  const void* f = pick_small(plain, winner, shade);
   if (!f) return cudaErrorInvalidValue;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, kWarps * 32, smem_bytes);
 }
 
 cudaError_t small_launch(bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int grid, int smem_bytes,
                          cudaStream_t stream) {
-  const void* f = pick_small(plain, winner, A.smooth_any != 0);
+  const void* f = pick_small(plain, winner, shade_of(A));
   if (!f) return cudaErrorInvalidValue;
   void* args[] = {const_cast<SceneParams*>(&P), const_cast<RasterArgs*>(&A)};
   return cudaLaunchKernel(f, dim3(grid), dim3(kWarps * 32), args, (size_t)smem_bytes, stream);

@@ -91,10 +91,47 @@ def test_textured_plain_path_and_kernel_choice(cuda, oracle):
     b = _textured_scene(n=16, seed=3, raster_method="plain")
     pb = _plain_parity(b, oracle)
     assert (a.render() == pb).all(dim=1).float().mean() > 0.99
-    # the scene-per-warp kernel does not draw textured nodes
+    # a scene too large for the scene-per-warp kernel is refused when that kernel is forced
     c = _textured_scene(n=4, seed=3, raster_kernel="warp")
     with pytest.raises(RuntimeError):
         c.render()
+
+
+def _small_textured(kernel, n=256, seed=21):
+    """CartPole-sized scenes (two textured boxes and a textured quad): within the
+    scene-per-warp kernel's limits."""
+    g = torch.Generator().manual_seed(seed)
+    r = pbr.PBRRenderer(num_scenes=n, tile_resolution=(64, 64), raster_kernel=kernel)
+    a = r.add_node("models/box", 1, model_pivot_relative_point=(0.5, 0.5, 0.5), model_scale=(1.5, 0.8, 0.6),
+                   texture=_texture(seed, 6, 10))
+    b = r.add_node("models/box", 1, model_pivot_relative_point=(0.5, 0.5, 0.0), model_scale=(0.3, 0.3, 2.0),
+                   texture=_texture(seed + 1, 16, 4))
+    q = r.add_node(_quad_mesh(), 1, model_pivot_relative_point=(0.5, 0.5, 0.5), model_scale=2.0,
+                   texture=_texture(seed + 2, 5, 5))
+    for node in (a, b, q):
+        node.set_positions(torch.rand((n, 3), generator=g) * 2 - 1)
+        node.set_hprs(torch.rand((n, 3), generator=g) * 6.3)
+        node.set_colors(torch.cat([torch.rand((n, 3), generator=g) * 0.5 + 0.5, torch.ones((n, 1))], 1))
+    r.add_camera(fov_y_deg=45.0)
+    r._pbr_cam.set_positions_and_lookat(torch.tensor([0.0, -7.0, 1.0]), torch.tensor([0.0, 0.0, 0.0]))
+    r.add_light()
+    r.setup_environment()
+    return r
+
+
+def test_small_textured_scenes_both_kernels(cuda, oracle):
+    """Textured CartPole-sized scenes: the scene-per-warp kernel draws them (its
+    textured instantiation), with the tile kernel's exact output and the
+    oracle's parity."""
+    w = _small_textured("warp")
+    t = _small_textured("tile")
+    pw, dw, ww = w.render(return_depth=True, return_winner=True)
+    pt, dt, wt = t.render(return_depth=True, return_winner=True)
+    assert torch.equal(pw, pt) and torch.equal(dw, dt) and torch.equal(ww, wt)
+    # randomly turned quads include near edge-on slivers: window depth to 1e-4
+    check_parity(w, oracle, depth_tol=1e-4)
+    a = _small_textured("auto")
+    assert torch.equal(a.render(), pw)
 
 
 def test_set_texture_after_setup(cuda, oracle):

@@ -321,11 +321,14 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
               const float wx = r0.x * b.x + r0.y * b.y + r0.z * b.z + r0.w;
               const float wy = r1.x * b.x + r1.y * b.y + r1.z * b.z + r1.w;
               const float wz = r2.x * b.x + r2.y * b.y + r2.z * b.z + r2.w;
-              // world radius: mesh radius times the largest column norm of the linear part
+              // world radius: mesh radius times the largest singular value of the linear part, which is
+              // the (common) column norm of a rotation times a uniform scale (HPR mode); other modes may
+              // hold any matrix, bounded by its Frobenius norm
               const float n0 = r0.x * r0.x + r1.x * r1.x + r2.x * r2.x;
               const float n1 = r0.y * r0.y + r1.y * r1.y + r2.y * r2.y;
               const float n2 = r0.z * r0.z + r1.z * r1.z + r2.z * r2.z;
-              const float R = b.w * sqrtf(fmaxf(fmaxf(n0, n1), n2)) * 1.0001f + 1e-6f;
+              const float sv2 = nd.mode == kModeHpr ? fmaxf(fmaxf(n0, n1), n2) : n0 + n1 + n2;
+              const float R = b.w * sqrtf(sv2) * 1.0001f + 1e-6f;
               const float cx = vp0 * wx + vp1 * wy + vp2 * wz + vp3, cy = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
               const float cw = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
               float xmin = 3.0e38f, xmax = -3.0e38f, ymin = 3.0e38f, ymax = -3.0e38f;

@@ -55,3 +55,23 @@ def test_node_table_limit_is_an_error(cuda):
     with pytest.raises(_capi.PBRError) as e:
         r.setup_environment()
     assert "nodes" in str(e.value)
+
+
+def test_tile_cull_with_sheared_transforms(cuda, oracle):
+    """Instances given as general (sheared, non-uniformly scaled) matrices: the
+    tile kernel's instance cull must stay conservative."""
+    n, inst = 8, 40
+    r = pbr.PBRRenderer(num_scenes=n, tile_resolution=(96, 96), raster_kernel="tile", raster_threads=128)
+    node = r.add_node("icosphere:1", inst, model_pivot_relative_point=(0.5, 0.5, 0.5))
+    g = torch.Generator().manual_seed(9)
+    B = node.buf_instances
+    M = torch.eye(4).repeat(B, 1, 1)
+    M[:, :3, :3] = torch.eye(3) * 0.6 + (torch.rand((B, 3, 3), generator=g) - 0.5) * 1.2  # shear + stretch
+    M[:, :3, 3] = torch.rand((B, 3), generator=g) * 10 - 5
+    node.set_transforms(M)
+    node.set_colors(torch.rand((B, 4), generator=g))
+    r.add_camera(fov_y_deg=60.0)
+    r._pbr_cam.set_positions_and_lookat(torch.tensor([0.0, -9.0, 0.0]), torch.tensor([0.0, 0.0, 0.0]))
+    r.add_light()
+    r.setup_environment()
+    check_parity(r, oracle, depth_tol=1e-4)

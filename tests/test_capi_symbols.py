@@ -56,3 +56,23 @@ def test_version_and_error_paths_without_gpu(lib):
     rc = lib.pbr_create(ctypes.byref(ctx), 4, 64, 64, 7, 0)
     assert rc == _capi.PBR_ERR_INVALID
     assert lib.pbr_render(None, None, None, None, None) == _capi.PBR_ERR_INVALID
+
+
+def test_cartpole_step_argument_checks_without_gpu(lib):
+    """pbr_cartpole_step validates its arguments before any CUDA call."""
+    f = lib.pbr_cartpole_step
+    f.restype = ctypes.c_int
+    f.argtypes = _capi.SIGNATURES["pbr_cartpole_step"]
+    consts = (ctypes.c_double * 9)(9.8, 1.0, 0.1, 0.5, 10.0, 0.02, 2.4, 0.2, 500)
+    p16, p20 = 0x10000, 0x10004  # aligned / misaligned stand-in addresses, never dereferenced
+    args = [p16, p16, None, None, None, None, None, p16, p16, p16, p16, p16]
+    assert f(*args, 0, consts, 0, None) == _capi.PBR_OK                     # no scenes: nothing to do
+    assert f(*args, -1, consts, 0, None) == _capi.PBR_ERR_INVALID
+    assert f(*args, 8, None, 0, None) == _capi.PBR_ERR_INVALID
+    assert f(*args, 8, consts, 1, None) == _capi.PBR_ERR_INVALID             # auto-reset needs the reset states
+    bad = list(args)
+    bad[0] = p20
+    assert f(*bad, 8, consts, 0, None) == _capi.PBR_ERR_INVALID              # [n,4] arrays must be 16-byte aligned
+    bad = list(args)
+    bad[1] = None
+    assert f(*bad, 8, consts, 0, None) == _capi.PBR_ERR_INVALID

@@ -75,3 +75,21 @@ def test_tile_cull_with_sheared_transforms(cuda, oracle):
     r.add_light()
     r.setup_environment()
     check_parity(r, oracle, depth_tol=1e-4)
+
+
+def test_capi_argument_errors(cuda):
+    """Invalid texture, bounds and coordinate arguments are errors with a message."""
+    import ctypes
+    r = _cubes(2, (32, 32), inst=1)
+    lib, ctx = r._lib, r._ctx
+    buf = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    assert lib.pbr_node_set_texture(ctx, 0, ctypes.c_void_p(buf.data_ptr()), 0, 4) == _capi.PBR_ERR_INVALID
+    assert b"texture size" in lib.pbr_last_error(ctx)
+    assert lib.pbr_node_set_texture(ctx, 0, ctypes.c_void_p(buf.data_ptr() + 1), 2, 2) == _capi.PBR_ERR_INVALID
+    assert lib.pbr_node_set_texture(ctx, 7, ctypes.c_void_p(buf.data_ptr()), 2, 2) == _capi.PBR_ERR_INVALID
+    assert lib.pbr_mesh_set_bounds(ctx, 0, 0.0, 0.0, 0.0, -1.0) == _capi.PBR_ERR_INVALID
+    assert lib.pbr_mesh_set_bounds(ctx, 0, float("nan"), 0.0, 0.0, 1.0) == _capi.PBR_ERR_INVALID
+    assert lib.pbr_mesh_set_uv(ctx, 0, ctypes.c_void_p(buf.data_ptr() + 4)) == _capi.PBR_ERR_INVALID
+    assert lib.pbr_mesh_set_uv(ctx, 3, None) == _capi.PBR_ERR_INVALID
+    # the context still renders afterwards
+    assert r.render().shape == (2, 3, 32, 32)

@@ -84,3 +84,25 @@ def test_kat_back_face_and_lit_face(cuda, kernel):
     assert int(cov.sum()) == 64
     for c in range(3):
         assert torch.all(pix[0, c][cov] == K.FACE_EXPECT[c])
+
+
+@pytest.mark.parametrize("kernel", ["warp", "tile", "binned"])
+def test_kat_soft_coverage(cuda, kernel):
+    """The soft known answers of tests/test_oracle_kat.py on each soft kernel:
+    half coverage on an edge, full coverage inside, background beyond the cut-off."""
+    r = pbr.PBRRenderer(num_scenes=2, tile_resolution=(K.W, K.H), raster_mode="soft", raster_kernel=kernel)
+    km = K.screen_mesh(K.SQUARE, K.SQUARE_TRIS)
+    node = r.add_node(Mesh(km.positions, km.normals, km.indices, name="kat"), 1, shared_across_scenes=True)
+    node.set_colors(torch.tensor((0.8, 0.4, 0.2, 1.0)))
+    r.add_camera()
+    r.add_light(strength=0.0)
+    r.setup_environment()
+    r._pbr_cam.VP_k44.copy_(torch.eye(4).expand(2, 4, 4))
+    with torch.no_grad():
+        out = r.render_soft()
+    col = torch.tensor([0.8, 0.4, 0.2], device="cuda")
+    for k in range(2):
+        assert torch.allclose(out[k, :, 8, 8], 0.5 * col, rtol=0, atol=2e-6)
+        assert torch.allclose(out[k, :, 4, 12], 0.5 * col, rtol=0, atol=2e-6)
+        assert torch.allclose(out[k, :, 7, 10], col, rtol=0, atol=2e-6)
+        assert torch.all(out[k, :, 2, 2] == 0.0) and torch.all(out[k, :, 20, 25] == 0.0)

@@ -77,3 +77,17 @@ def test_lit_face_colour(oracle):
     for c in range(3):
         assert np.all(ref["pixels"][0][c][cov] == K.FACE_EXPECT[c])
     assert K.FACE_EXPECT == (122, 184, 245)
+
+
+def test_soft_coverage_known_answers(oracle):
+    """Soft mode on the square (sigma = 0.5 / (2 ln 9) px, coverage cut off 16
+    sigma outside a triangle): a centre on one edge and far from the others is
+    half covered (sigmoid(0) = 1/2), a centre well inside is fully covered,
+    a centre beyond the cut-off sees only the background."""
+    mesh = K.screen_mesh(K.SQUARE, K.SQUARE_TRIS)
+    out = oracle.render_soft(K.scene(), [mesh], [K.node(0)], out_dtype=np.float64)[0]
+    col = np.array([0.8, 0.4, 0.2], np.float32).astype(np.float64)
+    assert np.allclose(out[:, 8, 8], 0.5 * col, rtol=0, atol=1e-7)     # (8.5, 8.5): on the left edge
+    assert np.allclose(out[:, 4, 12], 0.5 * col, rtol=0, atol=1e-7)    # (12.5, 4.5): on the top edge
+    assert np.allclose(out[:, 7, 10], col, rtol=0, atol=1e-6)          # 2 px or more from every edge
+    assert np.all(out[:, 2, 2] == 0.0) and np.all(out[:, 20, 25] == 0.0)  # beyond the cut-off

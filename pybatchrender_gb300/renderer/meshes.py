@@ -256,19 +256,81 @@ def load_egg(path: str) -> Mesh:
                 uvs=np.array(out_uv) if uvs else None, texture=texture)
 
 
-def load_gltf(path: str) -> Mesh:
-    """Minimal glTF 2.0 reader: first primitive of the first mesh (triangles),
-    POSITION / NORMAL / TEXCOORD_0 float accessors and an index accessor, data
-    in an external ``.bin`` buffer.  glTF puts ``v = 0`` at the top of the
-    image; the coordinates are flipped (``v -> 1 - v``) to the GL convention,
-    as Panda3D's glTF loader does.  A PNG ``baseColorTexture`` of the
-    primitive's material becomes the mesh's own texture."""
-    from .textures import load_image
+def _quat_matrix(q) -> np.ndarray:
+    x, y, z, w = (float(v) for v in q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
 
-    with open(path, "r", encoding="utf-8") as f:
-        doc = json.load(f)
+
+def _gltf_node_matrix(node: dict) -> np.ndarray:
+    """Local 4x4 transform of a glTF node: ``matrix`` (column-major) or T * R * S."""
+    if "matrix" in node:
+        return np.array(node["matrix"], dtype=np.float64).reshape(4, 4).T
+    m = np.eye(4)
+    m[:3, :3] = _quat_matrix(node.get("rotation", (0.0, 0.0, 0.0, 1.0))) @ np.diag(node.get("scale", (1.0, 1.0, 1.0)))
+    m[:3, 3] = node.get("translation", (0.0, 0.0, 0.0))
+    return m
+
+
+# glTF is Y-up, Panda3D Z-up: (x, y, z) -> (x, -z, y), a rotation about +x
+_YUP_TO_ZUP = np.array([[1.0, 0.0, 0.0, 0.0], [0.0, 0.0, -1.0, 0.0], [0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 0.0, 1.0]])
+
+
+def _read_gltf(path: str) -> tuple[dict, list[bytes], str]:
+    """(document, buffers, base directory) of a ``.gltf`` (external or base64
+    ``data:`` buffers) or a binary ``.glb`` container."""
+    import base64
+
     base = os.path.dirname(path)
-    buffers = [open(os.path.join(base, b["uri"]), "rb").read() for b in doc["buffers"]]
+    raw = open(path, "rb").read()
+    bin_chunk = None
+    if raw[:4] == b"glTF":
+        version, length = struct.unpack("<II", raw[4:12])
+        if version != 2:
+            raise ValueError(f"unsupported glb version {version}")
+        pos, doc = 12, None
+        while pos + 8 <= min(length, len(raw)):
+            clen, ctype = struct.unpack("<II", raw[pos:pos + 8])
+            body = raw[pos + 8:pos + 8 + clen]
+            if ctype == 0x4E4F534A:  # JSON
+                doc = json.loads(body.decode("utf-8"))
+            elif ctype == 0x004E4942:  # BIN
+                bin_chunk = body
+            pos += 8 + clen
+        if doc is None:
+            raise ValueError("glb without a JSON chunk")
+    else:
+        doc = json.loads(raw.decode("utf-8"))
+    buffers = []
+    for b in doc.get("buffers", []):
+        uri = b.get("uri")
+        if uri is None:
+            if bin_chunk is None:
+                raise ValueError("glTF buffer without a uri outside a glb container")
+            buffers.append(bin_chunk)
+        elif uri.startswith("data:"):
+            buffers.append(base64.b64decode(uri.split(",", 1)[1]))
+        else:
+            buffers.append(open(os.path.join(base, uri), "rb").read())
+    return doc, buffers, base
+
+
+def load_gltf(path: str) -> Mesh:
+    """glTF 2.0 reader (``.gltf`` with external or embedded buffers, ``.glb``):
+    every triangle primitive of every mesh reached from the default scene, with
+    its node transforms applied, flattened into one mesh as Panda3D's loader +
+    ``flattenStrong`` do; the file's Y-up axes become Panda3D's Z-up ones
+    ((x, y, z) -> (x, -z, y)).  POSITION / NORMAL / TEXCOORD_0 accessors;
+    missing normals are the area-weighted face normals.  glTF puts ``v = 0`` at
+    the top of the image; the coordinates are flipped (``v -> 1 - v``) to the GL
+    convention.  The first PNG ``baseColorTexture`` becomes the mesh's own
+    texture."""
+    import base64
+
+    from .textures import decode_png, load_image
+
+    doc, buffers, base = _read_gltf(path)
 
     def accessor(i: int) -> np.ndarray:
         acc = doc["accessors"][i]
@@ -286,38 +348,86 @@ def load_gltf(path: str) -> Mesh:
                             for k in range(acc["count"])])
         return arr.reshape(acc["count"], ncomp)
 
-    prim = doc["meshes"][0]["primitives"][0]
-    if prim.get("mode", 4) != 4:
-        raise ValueError("only triangle-list glTF primitives are supported")
-    p = accessor(prim["attributes"]["POSITION"]).astype(np.float32)
-    if "NORMAL" in prim["attributes"]:
-        n = accessor(prim["attributes"]["NORMAL"]).astype(np.float32)
+    def texture_of(prim) -> np.ndarray | None:
+        try:
+            mat = doc["materials"][prim["material"]]
+            tex = doc["textures"][mat["pbrMetallicRoughness"]["baseColorTexture"]["index"]]
+            img = doc["images"][tex["source"]]
+        except (KeyError, IndexError, TypeError):
+            return None
+        if "uri" in img:
+            if img["uri"].startswith("data:image/png;base64,"):
+                return decode_png(base64.b64decode(img["uri"].split(",", 1)[1]))
+            tex_path = os.path.join(base, img["uri"])
+            if os.path.isfile(tex_path) and tex_path.lower().endswith(".png"):
+                return load_image(tex_path)
+            return None
+        if img.get("mimeType") == "image/png" and "bufferView" in img:
+            bv = doc["bufferViews"][img["bufferView"]]
+            data = buffers[bv["buffer"]][bv.get("byteOffset", 0):bv.get("byteOffset", 0) + bv["byteLength"]]
+            return decode_png(data)
+        return None
+
+    parts_p, parts_n, parts_i, parts_uv = [], [], [], []
+    any_uv, texture, count = False, None, 0
+
+    def emit(mesh_index: int, world: np.ndarray) -> None:
+        nonlocal any_uv, texture, count
+        lin = world[:3, :3]
+        nmat = np.linalg.inv(lin).T if abs(np.linalg.det(lin)) > 0 else lin
+        flip = np.linalg.det(lin) < 0
+        for prim in doc["meshes"][mesh_index].get("primitives", []):
+            if prim.get("mode", 4) != 4:
+                raise ValueError("only triangle-list glTF primitives are supported")
+            p = accessor(prim["attributes"]["POSITION"]).astype(np.float64)
+            idx = accessor(prim["indices"]).reshape(-1, 3).astype(np.int64) if "indices" in prim else \
+                np.arange(len(p)).reshape(-1, 3)
+            if "NORMAL" in prim["attributes"]:
+                n = accessor(prim["attributes"]["NORMAL"]).astype(np.float64)
+            else:
+                n = np.zeros_like(p)
+            if not np.any(n):
+                tri = p[idx]
+                fn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+                for k in range(3):
+                    np.add.at(n, idx[:, k], fn)
+            uv = None
+            if "TEXCOORD_0" in prim["attributes"]:
+                t = accessor(prim["attributes"]["TEXCOORD_0"]).astype(np.float64)
+                uv = np.stack([t[:, 0], 1.0 - t[:, 1]], axis=1)
+                any_uv = True
+            parts_p.append(p @ world[:3, :3].T + world[:3, 3])
+            parts_n.append(n @ nmat.T)
+            parts_i.append((idx[:, [0, 2, 1]] if flip else idx) + count)
+            parts_uv.append(uv if uv is not None else np.zeros((len(p), 2)))
+            count += len(p)
+            if texture is None:
+                texture = texture_of(prim)
+
+    def walk(node_index: int, parent: np.ndarray, depth: int = 0) -> None:
+        if depth > 64:
+            raise ValueError("glTF node hierarchy too deep (a cycle?)")
+        node = doc["nodes"][node_index]
+        world = parent @ _gltf_node_matrix(node)
+        if "mesh" in node:
+            emit(node["mesh"], world)
+        for c in node.get("children", []):
+            walk(c, world, depth + 1)
+
+    scenes = doc.get("scenes")
+    if scenes:
+        for r in scenes[doc.get("scene", 0)].get("nodes", []):
+            walk(r, _YUP_TO_ZUP)
     else:
-        n = np.zeros_like(p)
-    idx = accessor(prim["indices"]).reshape(-1, 3).astype(np.int64) if "indices" in prim else \
-        np.arange(len(p)).reshape(-1, 3)
-    if not np.any(n):
-        n = np.zeros_like(p)
-        tri = p[idx]
-        fn = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
-        for k in range(3):
-            np.add.at(n, idx[:, k], fn)
+        for m in range(len(doc.get("meshes", []))):
+            emit(m, _YUP_TO_ZUP)
+    if not parts_p:
+        raise ValueError(f"no triangle geometry in {os.path.basename(path)}")
+    p = np.concatenate(parts_p)
+    n = np.concatenate(parts_n)
     n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-12)
-    uv = None
-    if "TEXCOORD_0" in prim["attributes"]:
-        t = accessor(prim["attributes"]["TEXCOORD_0"]).astype(np.float32)
-        uv = np.stack([t[:, 0], 1.0 - t[:, 1]], axis=1)
-    texture = None
-    try:
-        mat = doc["materials"][prim["material"]]
-        tex = doc["textures"][mat["pbrMetallicRoughness"]["baseColorTexture"]["index"]]
-        uri = doc["images"][tex["source"]]["uri"]
-        tex_path = os.path.join(base, uri)
-        if os.path.isfile(tex_path) and tex_path.lower().endswith(".png"):
-            texture = load_image(tex_path)
-    except (KeyError, IndexError, TypeError):
-        pass
-    return Mesh(p, n, idx.astype(np.int32), name=os.path.basename(path), uvs=uv, texture=texture)
+    return Mesh(p.astype(np.float32), n.astype(np.float32), np.concatenate(parts_i).astype(np.int32),
+                name=os.path.basename(path), uvs=np.concatenate(parts_uv) if any_uv else None, texture=texture)
 
 
 _BUILTIN = {
@@ -347,7 +457,7 @@ def resolve_model(model: "str | Mesh") -> Mesh:
         low = model.lower()
         if low.endswith(".egg"):
             return load_egg(model)
-        if low.endswith(".gltf"):
+        if low.endswith(".gltf") or low.endswith(".glb"):
             return load_gltf(model)
         raise ValueError(f"unsupported model file type: {model}")
     name = model

@@ -1,0 +1,77 @@
+"""glTF loading (CPU): scene traversal with node transforms (matrix and
+translation/rotation/scale), several primitives and meshes flattened into one
+mesh, the Y-up to Z-up axis change, embedded (data: URI) buffers and the binary
+.glb container, all giving the same mesh."""
+import base64
+import json
+import math
+import struct
+
+import numpy as np
+
+from pybatchrender_gb300.renderer import meshes
+
+TRI = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)  # in the z = 0 plane, normal +z (glTF frame)
+IDX = np.array([0, 1, 2], np.uint16)
+
+
+def _doc(uri):
+    blob = TRI.tobytes() + IDX.tobytes() + b"\x00\x00"
+    q = (math.sin(math.pi / 4), 0.0, 0.0, math.cos(math.pi / 4))  # +90 degrees about x
+    doc = {
+        "asset": {"version": "2.0"},
+        "buffers": [{"byteLength": len(blob)} if uri is None else {"uri": uri, "byteLength": len(blob)}],
+        "bufferViews": [{"buffer": 0, "byteOffset": 0, "byteLength": 36}, {"buffer": 0, "byteOffset": 36, "byteLength": 6}],
+        "accessors": [{"bufferView": 0, "componentType": 5126, "count": 3, "type": "VEC3"},
+                      {"bufferView": 1, "componentType": 5123, "count": 3, "type": "SCALAR"}],
+        "meshes": [{"primitives": [{"attributes": {"POSITION": 0}, "indices": 1},
+                                   {"attributes": {"POSITION": 0}, "indices": 1}]}],
+        "nodes": [
+            {"children": [1], "translation": [10.0, 0.0, 0.0]},
+            {"mesh": 0, "rotation": list(q), "scale": [2.0, 2.0, 2.0]},
+            {"mesh": 0, "matrix": [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 5, 0, 1]},  # column-major, +5 in y
+        ],
+        "scenes": [{"nodes": [0, 2]}], "scene": 0,
+    }
+    return doc, blob
+
+
+def _expected():
+    # node 0 -> 1: scale 2, rotate +90 deg about x ((x, y, z) -> (x, -z, y)), translate +10 x; twice (2 primitives)
+    a = TRI * 2.0
+    a = np.stack([a[:, 0], -a[:, 2], a[:, 1]], 1) + np.array([10.0, 0.0, 0.0])
+    b = TRI + np.array([0.0, 5.0, 0.0])
+    glb = np.concatenate([a, a, b, b])
+    return np.stack([glb[:, 0], -glb[:, 2], glb[:, 1]], 1)  # Y-up -> Z-up
+
+
+def test_gltf_scene_traversal_and_axes(tmp_path):
+    doc, blob = _doc("tri.bin")
+    (tmp_path / "tri.bin").write_bytes(blob)
+    (tmp_path / "s.gltf").write_text(json.dumps(doc))
+    m = meshes.resolve_model(str(tmp_path / "s.gltf"))
+    assert m.num_triangles == 4 and m.num_vertices == 12
+    assert np.allclose(m.positions, _expected(), atol=1e-6)
+    # flat face normals: the glTF +z normal of the plain copy becomes -y in Z-up
+    assert np.allclose(m.normals[6:], [[0.0, -1.0, 0.0]] * 6, atol=1e-6)
+    assert np.array_equal(m.indices, [[0, 1, 2], [3, 4, 5], [6, 7, 8], [9, 10, 11]])
+
+
+def test_gltf_embedded_and_glb_match(tmp_path):
+    doc, blob = _doc("tri.bin")
+    (tmp_path / "tri.bin").write_bytes(blob)
+    (tmp_path / "s.gltf").write_text(json.dumps(doc))
+    ref = meshes.resolve_model(str(tmp_path / "s.gltf"))
+    d2, _ = _doc("data:application/octet-stream;base64," + base64.b64encode(blob).decode())
+    (tmp_path / "e.gltf").write_text(json.dumps(d2))
+    e = meshes.resolve_model(str(tmp_path / "e.gltf"))
+    d3, _ = _doc(None)
+    js = json.dumps(d3).encode()
+    js += b" " * ((4 - len(js) % 4) % 4)
+    bn = blob + b"\x00" * ((4 - len(blob) % 4) % 4)
+    glb = (b"glTF" + struct.pack("<II", 2, 12 + 8 + len(js) + 8 + len(bn)) + struct.pack("<II", len(js), 0x4E4F534A) + js
+           + struct.pack("<II", len(bn), 0x004E4942) + bn)
+    (tmp_path / "s.glb").write_bytes(glb)
+    g = meshes.resolve_model(str(tmp_path / "s.glb"))
+    for m in (e, g):
+        assert np.array_equal(m.positions, ref.positions) and np.array_equal(m.indices, ref.indices)

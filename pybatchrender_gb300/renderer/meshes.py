@@ -203,57 +203,146 @@ def _triangulate_fan(poly: Sequence[int]) -> list[tuple[int, int, int]]:
     return [(poly[0], poly[i], poly[i + 1]) for i in range(1, len(poly) - 1)]
 
 
-def load_egg(path: str) -> Mesh:
-    """Minimal Panda3D ``.egg`` reader: one ``<VertexPool>`` of ``<Vertex>``
-    entries (position + optional ``<Normal>`` and ``<UV>``) and ``<Polygon>``
-    entries with ``<VertexRef>``.  Polygons are fan-triangulated; vertices
-    without a normal get the polygon's face normal.  The first ``<Texture>``
-    whose image file exists (PNG) becomes the mesh's own texture."""
+def _egg_tokens(text: str) -> list[str]:
     import re
+    return re.findall(r'"(?:[^"\\]|\\.)*"|<[^>]*>|[{}]|[^\s{}<"]+', text)
 
+
+def _egg_parse(tokens: list[str], i: int = 0, depth: int = 0) -> tuple[list, int]:
+    """Egg syntax tree: entries ``(tag, name, children)`` and loose value tokens."""
+    if depth > 256:
+        raise ValueError("egg nesting too deep")
+    items: list = []
+    while i < len(tokens):
+        t = tokens[i]
+        if t == "}":
+            return items, i + 1
+        if t.startswith("<") and t.endswith(">"):
+            tag, name = t[1:-1], None
+            i += 1
+            if i < len(tokens) and tokens[i] != "{":
+                name = tokens[i].strip('"')
+                i += 1
+            if i >= len(tokens) or tokens[i] != "{":
+                raise ValueError(f"egg: expected '{{' after <{tag}>")
+            children, i = _egg_parse(tokens, i + 1, depth + 1)
+            items.append((tag, name, children))
+        else:
+            items.append(t.strip('"'))
+            i += 1
+    if depth:
+        raise ValueError("egg: unbalanced braces")
+    return items, i
+
+
+def _egg_values(items) -> list[str]:
+    return [x for x in items if isinstance(x, str)]
+
+
+def _egg_entries(items, tag: str):
+    return [x for x in items if isinstance(x, tuple) and x[0].lower() == tag.lower()]
+
+
+def load_egg(path: str) -> Mesh:
+    """Panda3D ``.egg`` reader for static geometry: every ``<VertexPool>``
+    (vertices with an optional ``<Normal>`` and ``<UV>``), every ``<Polygon>``
+    at any ``<Group>`` depth with ``<VertexRef>`` into a named pool, flattened
+    into one mesh as ``flattenStrong`` does.  Egg vertices are written in the
+    model's coordinate space, so group ``<Transform>`` entries do not move
+    them.  Polygons are fan-triangulated; a vertex without a normal takes the
+    polygon's ``<Normal>`` or its face normal.  ``<CoordinateSystem> { Y-Up }``
+    files are turned to Panda3D's Z-up ((x, y, z) -> (x, -z, y)).  The first
+    referenced ``<Texture>`` whose image is a PNG becomes the mesh's own
+    texture."""
     from .textures import load_image
 
-    text = open(path, "r", encoding="utf-8").read()
-    pos: dict[int, tuple[float, float, float]] = {}
-    nrm: dict[int, tuple[float, float, float]] = {}
-    uvs: dict[int, tuple[float, float]] = {}
-    for m in re.finditer(r"<Vertex>\s*(\d+)\s*\{([^{}]*(?:\{[^{}]*\}[^{}]*)*)\}", text):
-        vid = int(m.group(1))
-        body = m.group(2)
-        head = body.split("<")[0].split()
-        pos[vid] = tuple(float(x) for x in head[:3])
-        nm = re.search(r"<Normal>\s*\{([^}]*)\}", body)
-        if nm:
-            nrm[vid] = tuple(float(x) for x in nm.group(1).split()[:3])
-        um = re.search(r"<UV>\s*(?:\w+\s*)?\{([^}]*)\}", body)
-        if um:
-            uvs[vid] = tuple(float(x) for x in um.group(1).split()[:2])
-    texture = None
-    for m in re.finditer(r"<Texture>\s*\S*\s*\{\s*\"?([^\"<}\s]+)\"?", text):
-        tex_path = os.path.join(os.path.dirname(path), m.group(1))
-        if os.path.isfile(tex_path) and tex_path.lower().endswith(".png"):
-            texture = load_image(tex_path)
-            break
-    polys = []
-    for m in re.finditer(r"<Polygon>\s*\{(.*?)<VertexRef>\s*\{([^}]*)\}", text, re.S):
-        refs = [int(x) for x in m.group(2).split("<")[0].split()]
-        polys.append(refs)
+    items, _ = _egg_parse(_egg_tokens(open(path, "r", encoding="utf-8").read()))
+    cs = "z-up"
+    for e in _egg_entries(items, "CoordinateSystem"):
+        cs = " ".join(_egg_values(e[2])).lower()
+    if cs not in ("z-up", "z-up-right", "y-up", "y-up-right"):
+        raise ValueError(f"unsupported egg coordinate system '{cs}'")
+    yup = cs.startswith("y-up")
+    textures: dict[str, str] = {}
+    pools: dict[str, dict[int, tuple]] = {}
+    polys: list[tuple[str, list[int], tuple | None, list[str]]] = []
+
+    def walk(entries, depth=0):
+        for e in entries:
+            if not isinstance(e, tuple):
+                continue
+            tag, name, children = e[0].lower(), e[1], e[2]
+            if tag == "texture":
+                vals = _egg_values(children)
+                if vals:
+                    textures[name or ""] = vals[0]
+            elif tag == "vertexpool":
+                pool = pools.setdefault(name or "", {})
+                for v in _egg_entries(children, "Vertex"):
+                    coords = [float(x) for x in _egg_values(v[2])]
+                    if len(coords) < 3:
+                        raise ValueError("egg vertex without three coordinates")
+                    if len(coords) == 4 and coords[3] not in (0.0, 1.0):
+                        coords = [c / coords[3] for c in coords[:3]]
+                    nrm = _egg_entries(v[2], "Normal")
+                    uv = _egg_entries(v[2], "UV")
+                    pool[int(v[1])] = (tuple(coords[:3]),
+                                       tuple(float(x) for x in _egg_values(nrm[0][2])[:3]) if nrm else None,
+                                       tuple(float(x) for x in _egg_values(uv[0][2])[:2]) if uv else None)
+            elif tag == "polygon":
+                refs = _egg_entries(children, "VertexRef")
+                if not refs:
+                    continue
+                ids = [int(x) for x in _egg_values(refs[0][2])]
+                pool_ref = _egg_entries(refs[0][2], "Ref")
+                pool_name = _egg_values(pool_ref[0][2])[0] if pool_ref else ""
+                pn = _egg_entries(children, "Normal")
+                tref = [t for r in _egg_entries(children, "TRef") for t in _egg_values(r[2])]
+                polys.append((pool_name, ids, tuple(float(x) for x in _egg_values(pn[0][2])[:3]) if pn else None, tref))
+            elif tag in ("group", "instance") and depth < 256:
+                walk(children, depth + 1)
+
+    walk(items)
     out_p, out_n, out_i, out_uv = [], [], [], []
-    for refs in polys:
-        pts = np.array([pos[r] for r in refs], float)
+    any_uv = False
+    used_tex: list[str] = []
+    for pool_name, ids, pnorm, tref in polys:
+        pool = pools.get(pool_name) if pool_name in pools else (next(iter(pools.values())) if len(pools) == 1 else None)
+        if pool is None:
+            raise ValueError(f"egg polygon refers to unknown vertex pool '{pool_name}'")
+        if len(ids) < 3:
+            continue
+        pts = np.array([pool[r][0] for r in ids], float)
         fn = np.cross(pts[1] - pts[0], pts[2] - pts[0])
         ln = np.linalg.norm(fn)
         fn = fn / ln if ln > 0 else np.array([0.0, 0.0, 1.0])
         base = len(out_p)
-        for r in refs:
-            out_p.append(pos[r])
-            out_n.append(nrm.get(r, tuple(fn)))
-            out_uv.append(uvs.get(r, (0.0, 0.0)))
-        out_i += _triangulate_fan(list(range(base, base + len(refs))))
+        for r in ids:
+            p, nrm, uv = pool[r]
+            out_p.append(p)
+            out_n.append(nrm if nrm is not None else (pnorm if pnorm is not None else tuple(fn)))
+            out_uv.append(uv if uv is not None else (0.0, 0.0))
+            any_uv = any_uv or uv is not None
+        out_i += _triangulate_fan(list(range(base, base + len(ids))))
+        used_tex += [t for t in tref if t not in used_tex]
+    if not out_p:
+        raise ValueError(f"no polygons in {os.path.basename(path)}")
+    texture = None
+    for t in used_tex + [k for k in textures if k not in used_tex]:
+        rel = textures.get(t)
+        if rel:
+            tex_path = os.path.join(os.path.dirname(path), rel)
+            if os.path.isfile(tex_path) and tex_path.lower().endswith(".png"):
+                texture = load_image(tex_path)
+                break
+    p = np.array(out_p, float)
     n = np.array(out_n, float)
+    if yup:
+        p = np.stack([p[:, 0], -p[:, 2], p[:, 1]], 1)
+        n = np.stack([n[:, 0], -n[:, 2], n[:, 1]], 1)
     n /= np.maximum(np.linalg.norm(n, axis=1, keepdims=True), 1e-12)
-    return Mesh(np.array(out_p), n, np.array(out_i), name=os.path.basename(path),
-                uvs=np.array(out_uv) if uvs else None, texture=texture)
+    return Mesh(p, n, np.array(out_i), name=os.path.basename(path),
+                uvs=np.array(out_uv) if any_uv else None, texture=texture)
 
 
 def _quat_matrix(q) -> np.ndarray:

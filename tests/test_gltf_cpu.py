@@ -1,4 +1,4 @@
-"""glTF loading (CPU): scene traversal with node transforms (matrix and
+"""Model loading (CPU). glTF: scene traversal with node transforms (matrix and
 translation/rotation/scale), several primitives and meshes flattened into one
 mesh, the Y-up to Z-up axis change, embedded (data: URI) buffers and the binary
 .glb container, all giving the same mesh."""
@@ -8,6 +8,7 @@ import math
 import struct
 
 import numpy as np
+import pytest
 
 from pybatchrender_gb300.renderer import meshes
 
@@ -75,3 +76,43 @@ def test_gltf_embedded_and_glb_match(tmp_path):
     g = meshes.resolve_model(str(tmp_path / "s.glb"))
     for m in (e, g):
         assert np.array_equal(m.positions, ref.positions) and np.array_equal(m.indices, ref.indices)
+
+
+EGG = """<CoordinateSystem> { %s }
+<Comment> { "two pools, nested groups, a polygon normal" }
+<Group> root {
+  <Transform> { <Translate> { 5 0 0 } }
+  <VertexPool> a {
+    <Vertex> 0 { 0 0 0 }
+    <Vertex> 1 { 1 0 0 }
+    <Vertex> 2 { 1 1 0 <UV> { 0.5 0.25 } }
+  }
+  <Group> inner {
+    <VertexPool> b {
+      <Vertex> 7 { 0 0 1 <Normal> { 0 0 1 } }
+      <Vertex> 8 { 1 0 1 <Normal> { 0 0 1 } }
+      <Vertex> 9 { 1 1 1 <Normal> { 0 0 1 } }
+      <Vertex> 10 { 0 1 1 <Normal> { 0 0 1 } }
+    }
+    <Polygon> { <Normal> { 0 0 -1 } <VertexRef> { 0 1 2 <Ref> { a } } }
+    <Polygon> { <VertexRef> { 7 8 9 10 <Ref> { b } } }
+  }
+}
+"""
+
+
+def test_egg_pools_groups_and_axes(tmp_path):
+    (tmp_path / "z.egg").write_text(EGG % "Z-Up")
+    m = meshes.resolve_model(str(tmp_path / "z.egg"))
+    assert m.num_triangles == 3 and m.num_vertices == 7
+    # vertex positions are in model space: the group transform does not move them
+    assert np.allclose(m.positions[:3], [[0, 0, 0], [1, 0, 0], [1, 1, 0]])
+    assert np.allclose(m.normals[:3], [[0, 0, -1]] * 3)       # the polygon's own normal
+    assert np.allclose(m.normals[3:], [[0, 0, 1]] * 4)        # the vertices' normals
+    assert np.allclose(m.uvs[2], [0.5, 0.25]) and np.allclose(m.uvs[0], [0.0, 0.0])
+    (tmp_path / "y.egg").write_text(EGG % "Y-Up")
+    y = meshes.resolve_model(str(tmp_path / "y.egg"))
+    assert np.allclose(y.positions, np.stack([m.positions[:, 0], -m.positions[:, 2], m.positions[:, 1]], 1))
+    (tmp_path / "bad.egg").write_text((EGG % "Z-Up").replace("<Ref> { b }", "<Ref> { nope }"))
+    with pytest.raises(ValueError):
+        meshes.resolve_model(str(tmp_path / "bad.egg"))

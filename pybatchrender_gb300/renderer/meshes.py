@@ -430,12 +430,17 @@ def load_gltf(path: str) -> Mesh:
         itemsize = np.dtype(comp).itemsize * ncomp
         stride = bv.get("byteStride", itemsize)
         raw = buffers[bv["buffer"]]
+        if "sparse" in acc:
+            raise ValueError("sparse glTF accessors are not supported")
         if stride == itemsize:
             arr = np.frombuffer(raw, dtype=comp, count=acc["count"] * ncomp, offset=off)
         else:
             arr = np.stack([np.frombuffer(raw, dtype=comp, count=ncomp, offset=off + k * stride)
                             for k in range(acc["count"])])
-        return arr.reshape(acc["count"], ncomp)
+        arr = arr.reshape(acc["count"], ncomp)
+        if acc.get("normalized") and comp is not np.float32:
+            arr = arr.astype(np.float64) / float(np.iinfo(comp).max)  # unsigned normalised integers
+        return arr
 
     def texture_of(prim) -> np.ndarray | None:
         try:

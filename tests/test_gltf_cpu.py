@@ -116,3 +116,18 @@ def test_egg_pools_groups_and_axes(tmp_path):
     (tmp_path / "bad.egg").write_text((EGG % "Z-Up").replace("<Ref> { b }", "<Ref> { nope }"))
     with pytest.raises(ValueError):
         meshes.resolve_model(str(tmp_path / "bad.egg"))
+
+
+def test_gltf_normalized_texcoords(tmp_path):
+    doc, blob = _doc("tri.bin")
+    uv16 = np.array([[0, 0], [65535, 0], [0, 32768]], np.uint16)
+    blob2 = blob + uv16.tobytes()
+    doc["buffers"][0]["byteLength"] = len(blob2)
+    doc["bufferViews"].append({"buffer": 0, "byteOffset": len(blob), "byteLength": 12})
+    doc["accessors"].append({"bufferView": 2, "componentType": 5123, "count": 3, "type": "VEC2", "normalized": True})
+    doc["meshes"][0]["primitives"] = [{"attributes": {"POSITION": 0, "TEXCOORD_0": 2}, "indices": 1}]
+    doc["scenes"][0]["nodes"] = [2]
+    (tmp_path / "tri.bin").write_bytes(blob2)
+    (tmp_path / "u.gltf").write_text(json.dumps(doc))
+    m = meshes.resolve_model(str(tmp_path / "u.gltf"))
+    assert np.allclose(m.uvs, [[0.0, 1.0], [1.0, 1.0], [0.0, 1.0 - 32768 / 65535]], atol=1e-6)

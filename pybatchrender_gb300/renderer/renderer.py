@@ -251,6 +251,8 @@ class PBRRenderer:
         ``[N,C,H,W]`` on the CUDA device (plus float32 ``[N,H,W]`` depth when
         ``cfg.return_depth``), ``None`` when ``return_pixels`` is False
         (``renderer.py:377-390``)."""
+        if self.cfg.report_fps:
+            self.report_fps()
         fused = return_pixels and not self.cfg.interactive and self.cfg.raster_method == "batched" \
             and self.cfg.raster_mode == "hard"
         if fused:
@@ -622,6 +624,20 @@ class PBRRenderer:
         except Exception:
             pass
 
-    # reference compatibility (Panda3D task manager / FPS report)
     def report_fps(self, task=None):
-        return None
+        """``renderer.py:242-251``: count frames and, every
+        ``cfg.report_fps_interval`` seconds, print the scene frames per second
+        (steps per second times ``num_scenes``) since the previous report.
+        Called by ``step`` when ``cfg.report_fps`` is set; host time, so a
+        queue of launches that have not run yet counts as done."""
+        import time
+        now = time.perf_counter()
+        if getattr(self, "_fps_t0", None) is None:
+            self._fps_t0, self._fps_frames = now, 0
+            return getattr(task, "cont", None)
+        self._fps_frames += 1
+        if now - self._fps_t0 >= float(self.cfg.report_fps_interval):
+            fps = self._fps_frames * self.num_scenes / (now - self._fps_t0)
+            print(f"FPS: {fps:.1f}")
+            self._fps_t0, self._fps_frames = now, 0
+        return getattr(task, "cont", None)

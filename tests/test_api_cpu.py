@@ -214,3 +214,14 @@ def test_manual_camera_control_headless():
     r.update_camera(dt=0.1)
     eye1 = cam.get_eye().reshape(-1, 3)
     assert torch.allclose(eye1 - eye0, torch.tensor([[-2.5, 2.5, 0.0]]).expand(2, 3))
+
+
+def test_report_fps_prints(capsys):
+    r = pbr.PBRRenderer(num_scenes=10, device="cpu", report_fps_interval=0.0)
+    r.report_fps()
+    r.report_fps()
+    out = capsys.readouterr().out
+    assert out.startswith("FPS: ")
+    q = pbr.PBRRenderer(num_scenes=10, device="cpu", report_fps=False)
+    q.step(return_pixels=False)
+    assert capsys.readouterr().out == ""

@@ -112,3 +112,24 @@ def test_template_env_renders(cuda, oracle):
     nxt = env.step(td)["next"]
     assert not torch.equal(nxt["pixels"], td["pixels"])
     check_parity(env._renderer, oracle)
+
+
+def test_template_env_in_graph(cuda):
+    """GraphedEnvStep over the template environment: same observations and
+    pixels as the eager step (no auto-reset, so no random draws)."""
+    from pybatchrender_gb300.envs._template import MyEnv, MyEnvConfig, MyEnvRenderer
+    cfg = MyEnvConfig(num_scenes=64, device="cuda", auto_reset=False)
+    eager = MyEnv(MyEnvRenderer(cfg), cfg)
+    graphed = MyEnv(MyEnvRenderer(cfg), cfg)
+    g = pbr.GraphedEnvStep(graphed)
+    td = eager.reset()
+    obs, sc = td["observation"].clone(), td["step_count"].clone()
+    ob_e, sc_e, ob_g, sc_g = obs, sc, obs.clone(), sc.clone()
+    for i in range(5):
+        act = (torch.arange(64, device="cuda") + i) % 2
+        e = eager._step(pbr.env.TensorDict({"observation": ob_e, "action": act, "step_count": sc_e}, batch_size=[64]))
+        o = g({"observation": ob_g, "action": act, "step_count": sc_g})
+        for key in ("observation", "reward", "done", "step_count", "pixels"):
+            assert torch.equal(e[key], o[key]), key
+        ob_e, sc_e = e["observation"], e["step_count"]
+        ob_g, sc_g = o["observation"].clone(), o["step_count"].clone()

@@ -15,6 +15,7 @@ from .renderer import PBRCam, PBRLight, PBRNode, PBRRenderer, PBRShaderContext  
 from ._capi import PBRError, RendererUnavailable  # noqa: F401
 from .env import GraphedEnvStep, PBREnv  # noqa: F401
 from . import envs  # noqa: F401
+from .compat import install_as_pybatchrender  # noqa: F401
 
 GPUFrameGrabber = None
 CPUFrameGrabber = None
@@ -28,5 +29,5 @@ except Exception:  # pragma: no cover
 __all__ = [
     "PBRConfig", "PBREnv", "GraphedEnvStep", "PBRRenderer", "PBRNode", "PBRCam", "PBRLight", "PBRShaderContext",
     "GPUFrameGrabber", "CPUFrameGrabber", "FrameGrabber", "envs", "__version__", "PBRError",
-    "RendererUnavailable",
+    "RendererUnavailable", "install_as_pybatchrender",
 ]

@@ -118,9 +118,10 @@ def test_template_env_in_graph(cuda):
     """GraphedEnvStep over the template environment: same observations and
     pixels as the eager step (no auto-reset, so no random draws)."""
     from pybatchrender_gb300.envs._template import MyEnv, MyEnvConfig, MyEnvRenderer
-    cfg = MyEnvConfig(num_scenes=64, device="cuda", auto_reset=False)
-    eager = MyEnv(MyEnvRenderer(cfg), cfg)
-    graphed = MyEnv(MyEnvRenderer(cfg), cfg)
+    def make():
+        cfg = MyEnvConfig(num_scenes=64, device="cuda", auto_reset=False)
+        return MyEnv(MyEnvRenderer(cfg), cfg)
+    eager, graphed = make(), make()
     g = pbr.GraphedEnvStep(graphed)
     td = eager.reset()
     obs, sc = td["observation"].clone(), td["step_count"].clone()

@@ -67,3 +67,39 @@ def unorm8(v: float) -> int:
 FACE_COLOR = (0.4, 0.6, 0.8, 1.0)
 FACE_AMBIENT = (0.2, 0.2, 0.2)
 FACE_EXPECT = tuple(unorm8(np.float32(c) * (np.float32(0.2) + np.float32(1.0))) for c in FACE_COLOR[:3])
+
+
+def textured_square(uvs, z=0.25) -> KMesh:
+    """The square with per-corner texture coordinates (BL, BR, TR, TL)."""
+    m = screen_mesh(SQUARE, SQUARE_TRIS, z=z)
+    m.uvs = np.asarray(uvs, np.float32).reshape(4, 2)
+    return m
+
+
+def texture(rgb_rows) -> np.ndarray:
+    """[h][w] lists of (r, g, b) -> an RGBA8 texture [h, w, 4], row 0 at v = 0."""
+    t = np.asarray(rgb_rows, np.uint8)
+    return np.concatenate([t, np.full(t.shape[:2] + (1,), 255, np.uint8)], axis=2)
+
+
+# A plane seen in perspective: clip = (x, y, z - 2, z), so NDC x = x / z.
+# The quad's left edge lies at NDC x = -0.5 and depth z0, its right edge at
+# NDC x = +0.5 and depth z1 (two vertical segments, so the quad is planar).
+PERSP_Z0, PERSP_Z1 = 1.5, 3.0
+PERSP_VP = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 1, -2], [0, 0, 1, 0]], np.float32)  # ndc z = 1 - 2 / z
+
+
+def perspective_quad() -> KMesh:
+    z0, z1 = PERSP_Z0, PERSP_Z1
+    pts = [(-0.5 * z0, -0.5 * z0, z0), (0.5 * z1, -0.5 * z1, z1), (0.5 * z1, 0.5 * z1, z1), (-0.5 * z0, 0.5 * z0, z0)]
+    m = KMesh(pts, SQUARE_TRIS)
+    m.uvs = np.array([(0, 0), (1, 0), (1, 1), (0, 1)], np.float32)
+    return m
+
+
+def perspective_u(ndc_x):
+    """u at NDC x on the quad: u = (z - z0) / (z1 - z0) is affine in world
+    space, and the point of the plane seen at NDC x solves
+    ndc_x * z(u) = x(u), which gives u = z0 (0.5 + ndc_x) / (0.5 (z0 + z1) - ndc_x (z1 - z0))."""
+    z0, z1 = PERSP_Z0, PERSP_Z1
+    return z0 * (0.5 + ndc_x) / (0.5 * (z0 + z1) - ndc_x * (z1 - z0))

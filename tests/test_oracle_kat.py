@@ -1,8 +1,10 @@
 """Known-answer tests that pin the oracle's raster rules (CPU): the top-left
 fill rule on edges through pixel centres, watertight shared edges (every
 centre on a shared edge belongs to exactly one triangle), degenerate and
-sliver triangles that cover no centre, exact window depth, back-face culling
-and an analytically shaded face."""
+sliver triangles that cover no centre, exact window depth, back-face culling,
+an analytically shaded face, GL_LINEAR + GL_REPEAT texture sampling with
+row 0 at v = 0, per-fragment renormalised smooth normals and
+perspective-correct texture coordinates."""
 import numpy as np
 import pytest
 
@@ -91,3 +93,98 @@ def test_soft_coverage_known_answers(oracle):
     assert np.allclose(out[:, 4, 12], 0.5 * col, rtol=0, atol=1e-7)    # (12.5, 4.5): on the top edge
     assert np.allclose(out[:, 7, 10], col, rtol=0, atol=1e-6)          # 2 px or more from every edge
     assert np.all(out[:, 2, 2] == 0.0) and np.all(out[:, 20, 25] == 0.0)  # beyond the cut-off
+
+
+def test_texture_bilinear_repeat_along_u(oracle):
+    """A 2 x 1 texture (texel 0 black, texel 1 = 200) stretched over the
+    square with u = 0 .. 1 left to right.  Pixel column c samples
+    u = (c - 8) / 8, i.e. texel x = 2u - 0.5; GL_LINEAR with GL_REPEAT blends
+    texel 1 into the left half-texel and the right half-texel wraps to texel 0."""
+    mesh = K.textured_square([(0, 0), (1, 0), (1, 1), (0, 1)])
+    nd = K.node(0, color=(1.0, 1.0, 1.0, 1.0))
+    nd["texture"] = K.texture([[(0, 0, 0), (200, 100, 40)]])
+    ref = _render(oracle, K.scene(), [mesh], [nd])
+    cov = ref["winner"][0] >= 0
+    assert np.array_equal(cov, K.square_expected())
+    # texel x = -0.5, -0.25, 0, 0.25, 0.5, 0.75, 1, 1.25 -> weight of texel 1
+    w1 = np.array([0.5, 0.25, 0.0, 0.25, 0.5, 0.75, 1.0, 0.75])
+    for c, full in enumerate((200, 100, 40)):
+        expect = np.floor(w1 * full + 0.5).astype(np.uint8)
+        assert np.all(ref["pixels"][0][c][4:12, 8:16] == expect[None, :]), c
+
+
+def test_texture_row_zero_is_at_the_bottom(oracle):
+    """A 1 x 2 texture: row 0 (v = 0) is drawn at the bottom of the square.
+    Pixel row r samples v = (12 - r) / 8, texel y = 2v - 0.5."""
+    mesh = K.textured_square([(0, 0), (1, 0), (1, 1), (0, 1)])
+    nd = K.node(0, color=(1.0, 1.0, 1.0, 1.0))
+    nd["texture"] = K.texture([[(0, 200, 0)], [(200, 0, 0)]])
+    ref = _render(oracle, K.scene(), [mesh], [nd])
+    # rows 4..11: texel y = 1.5, 1.25, 1, 0.75, 0.5, 0.25, 0, -0.25 -> weight of row 1
+    w1 = np.array([0.5, 0.75, 1.0, 0.75, 0.5, 0.25, 0.0, 0.25])
+    red = np.floor(w1 * 200 + 0.5).astype(np.uint8)
+    green = np.floor((1 - w1) * 200 + 0.5).astype(np.uint8)
+    assert np.all(ref["pixels"][0][0][4:12, 8:16] == red[:, None])
+    assert np.all(ref["pixels"][0][1][4:12, 8:16] == green[:, None])
+    assert np.all(ref["pixels"][0][2][4:12, 8:16] == 0)
+
+
+def test_texture_colour_is_modulated_by_instance_colour_and_light(oracle):
+    """Texel colour times instance colour times (ambient + n.l light)."""
+    mesh = K.textured_square([(0.5, 0.5)] * 4)  # one uv: the texel centre of a 1 x 1 texture
+    nd = K.node(0, color=K.FACE_COLOR)
+    nd["texture"] = K.texture([[(255, 255, 255)]])
+    sc = K.scene(strength=1.0, ambient=K.FACE_AMBIENT, ldir=(0.0, 0.0, 2.0), lcol=(1.0, 1.0, 1.0))
+    ref = _render(oracle, sc, [mesh], [nd])
+    cov = ref["winner"][0] >= 0
+    for c in range(3):
+        assert np.all(ref["pixels"][0][c][cov] == K.FACE_EXPECT[c])
+    nd["texture"] = K.texture([[(0, 255, 0)]])
+    ref = _render(oracle, sc, [mesh], [nd])
+    assert np.all(ref["pixels"][0][0][cov] == 0) and np.all(ref["pixels"][0][2][cov] == 0)
+    assert np.all(ref["pixels"][0][1][cov] == K.FACE_EXPECT[1])
+
+
+def test_smooth_normals_are_interpolated_and_renormalised(oracle):
+    """Vertex normals (-1, 0, 1) on the left corners and (1, 0, 1) on the
+    right: at pixel column c the fragment normal is (2t - 1, 0, 1) up to
+    scale with t = (c - 8) / 8, so n.l = 1 / sqrt((2t - 1)^2 + 1) for a
+    light along +z (per-fragment renormalisation, not a lerp of n.l)."""
+    mesh = K.screen_mesh(K.SQUARE, K.SQUARE_TRIS)
+    mesh.normals = np.array([(-1, 0, 1), (1, 0, 1), (1, 0, 1), (-1, 0, 1)], np.float32)
+    sc = K.scene(strength=1.0, ambient=(0.0, 0.0, 0.0), ldir=(0.0, 0.0, 1.0), lcol=(1.0, 1.0, 1.0))
+    ref = _render(oracle, sc, [mesh], [K.node(0, color=(1.0, 1.0, 1.0, 1.0))])
+    t = (np.arange(8, 16) - 8) / 8.0
+    ndl = 1.0 / np.sqrt((2 * t - 1) ** 2 + 1)
+    expect = np.floor(ndl * 255 + 0.5)
+    assert np.all(np.abs(ndl * 255 + 0.5 - np.round(ndl * 255 + 0.5)) > 1e-3)  # no value sits on a rounding tie
+    for c in range(3):
+        assert np.all(ref["pixels"][0][c][4:12, 8:16] == expect.astype(np.uint8)[None, :])
+    # per-vertex n.l interpolated linearly would give 1/sqrt(2) at both edges and in between
+    assert expect[4] == 255 and expect[0] == 180
+
+
+def test_perspective_correct_texture_coordinates(oracle):
+    """A quad whose right edge is twice as far as its left, textured with a
+    64-texel ramp (texel i = 4 i): the sampled value at NDC x is
+    256 u - 2 with u the perspective-correct coordinate, which differs from
+    the screen-affine one by up to 43 levels in the middle of the quad."""
+    mesh = K.perspective_quad()
+    nd = K.node(0, color=(1.0, 1.0, 1.0, 1.0))
+    ramp = [[(4 * i, 0, 0) for i in range(64)]]
+    nd["texture"] = K.texture(ramp)
+    ref = _render(oracle, K.scene(vp=K.PERSP_VP), [mesh], [nd])
+    cov = ref["winner"][0] >= 0
+    rows, cols = np.nonzero(cov)
+    assert rows.min() == 8 and rows.max() == 23 and cols.min() == 8 and cols.max() == 23
+    ndc_x = 2.0 * (np.arange(8, 24) + 0.5) / K.W - 1.0
+    u = K.perspective_u(ndc_x)
+    value = 256.0 * u - 2.0
+    inner = (u * 64 - 0.5 >= 0) & (u * 64 - 0.5 <= 63)  # away from the repeat seam
+    got = ref["pixels"][0][0][8:24, 8:24].astype(np.float64)
+    assert np.all(np.abs(got[:, inner] - value[None, inner]) <= 0.5 + 1e-6)
+    affine = 256.0 * (ndc_x + 0.5) - 2.0
+    assert np.max(np.abs(affine - value)[inner]) > 40
+    # window depth is the plane's: 0.5 (1 - 2 / z) + 0.5 with z = z0 + (z1 - z0) u
+    z = K.PERSP_Z0 + (K.PERSP_Z1 - K.PERSP_Z0) * u
+    assert np.allclose(ref["depth"][0][8:24, 8:24], (1.0 - 1.0 / z)[None, :], rtol=0, atol=1e-6)

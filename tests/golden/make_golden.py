@@ -5,7 +5,9 @@ checkout at ``/root/reference``) under the stand-ins of ``stub_panda3d.py`` and
 records what it would upload to OpenGL.  The fixtures pin everything before
 rasterisation: baked vertices, per-instance model matrices and colours,
 per-scene view-projection matrices, tile rectangles, shader uniforms and the
-``PBRConfig`` resolution bookkeeping.  Usage (from the repository root):
+``PBRConfig`` resolution bookkeeping.  ``ref_env_dynamics.npz`` records
+trajectories of the reference's CartPole and Steering environments
+(observations, rewards, done flags and step counters) from seeded inputs.  Usage (from the repository root):
 
     python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -52,8 +54,79 @@ def camera_record(cam, N: int) -> dict:
     return {"VP": vp, "tiles": cam.tilebuf.array((N, 4)), "P": cam.P_k44.numpy()}
 
 
+def cartpole_trajectory(cp, B: int = 64, T: int = 60) -> dict:
+    """The reference's CartPoleEnv._step (no rendering, no auto-reset) from
+    seeded states and actions: dynamics, termination (including the step
+    limit) and reward."""
+    env = cp.CartPoleEnv(renderer=None, cfg=cp.CartPoleConfig(num_scenes=B, device="cpu", render=False,
+                                                               auto_reset=False))
+    g = torch.Generator().manual_seed(11)
+    u = lambda lo, hi: torch.rand(B, generator=g) * (hi - lo) + lo  # noqa: E731
+    obs = torch.stack([u(-2.6, 2.6), u(-2.0, 2.0), u(-0.25, 0.25), u(-2.0, 2.0)], dim=-1)
+    sc = torch.randint(0, 520, (B,), generator=g)
+    actions = torch.randint(0, 2, (T, B), generator=g)
+    rec = {"cp_obs0": obs.numpy(), "cp_sc0": sc.numpy(), "cp_actions": actions.numpy()}
+    outs = {"observation": [], "reward": [], "done": [], "step_count": []}
+    for t in range(T):
+        td = env._step({"observation": obs, "step_count": sc, "action": actions[t]})
+        for k in outs:
+            outs[k].append(td[k].numpy())
+        obs, sc = td["observation"], td["step_count"]
+    rec.update({f"cp_{k}": np.stack(v) for k, v in outs.items()})
+    return rec
+
+
+def steering_trajectory(B: int = 32, T: int = 200) -> dict:
+    """The reference's SteeringEnv._step (no rendering, no auto-reset) from a
+    seeded world: 20 obstacles, a 300-step limit, continuous steering."""
+    st = sys.modules["pybatchrender.envs.steering"]
+    cfg = st.SteeringConfig(num_scenes=B, device="cpu", render=False, auto_reset=False, number_of_obstacles=20,
+                            max_steps=300)
+    env = st.SteeringEnv(renderer=None, cfg=cfg)
+    g = torch.Generator().manual_seed(12)
+    n = env.number_of_obstacles
+    xs = torch.tensor(env.obstacle_x_positions, dtype=torch.float32)
+    obstacles = torch.zeros(B, n, 4)
+    obstacles[:, :, 0] = xs[torch.randint(0, len(xs), (B, n), generator=g)]
+    obstacles[:, :, 1] = torch.arange(n, dtype=torch.float32) * env.obstacle_y_spacing + env.distance_to_first_obstacle
+    obstacles[:, :, 2] = (torch.rand(B, n, generator=g) < env.prob_gold).float()
+    obstacles[:, :, 3] = (torch.rand(B, n, generator=g) < env.prob_cone).float()
+    player_x = torch.rand(B, generator=g) * (env.x_max - env.x_min) + env.x_min
+    sc = torch.randint(0, 300, (B,), generator=g)
+    actions = (torch.rand(T, B, 1, generator=g) * 2 - 1) * env.action_high
+    rec = {"st_obstacles": obstacles.numpy(), "st_player_x0": player_x.numpy(), "st_sc0": sc.numpy(),
+           "st_actions": actions.numpy()}
+    env._obstacles = obstacles.clone()
+    env._player_x = player_x.clone()
+    env._player_y = torch.zeros(B)
+    env._prev_player_x = torch.zeros(B)
+    env._prev_player_y = torch.zeros(B)
+    env._forward_speed = torch.full((B,), env.speed_initial)
+    env._grace_remaining = torch.zeros(B)
+    env._next_obstacle_idx = torch.zeros(B, dtype=torch.long)
+    obs = env._get_observation()
+    rec["st_obs0"] = obs.numpy()
+    outs = {"observation": [], "reward": [], "done": [], "step_count": []}
+    grace, idx = [], []
+    for t in range(T):
+        td = env._step({"observation": obs, "step_count": sc, "action": actions[t]})
+        for k in outs:
+            outs[k].append(td[k].numpy())
+        grace.append(env._grace_remaining.numpy().copy())
+        idx.append(env._next_obstacle_idx.numpy().copy())
+        obs, sc = td["observation"], td["step_count"]
+    rec.update({f"st_{k}": np.stack(v) for k, v in outs.items()})
+    rec["st_grace"], rec["st_next_idx"] = np.stack(grace), np.stack(idx)
+    return rec
+
+
 def main(ref_path: str) -> None:
     pbr, cp = import_reference(ref_path)
+    with contextlib.redirect_stdout(io.StringIO()):
+        import pybatchrender.envs.steering  # noqa: F401
+        rec = cartpole_trajectory(cp)
+        rec.update(steering_trajectory())
+    np.savez_compressed(os.path.join(HERE, "ref_env_dynamics.npz"), **rec)
     with contextlib.redirect_stdout(io.StringIO()):
         for N, keep in ((5, None), (64, None), (4098, 16)):
             r = cp.CartPoleRenderer(cp.CartPoleConfig(num_scenes=N))

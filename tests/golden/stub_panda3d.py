@@ -384,11 +384,16 @@ def install() -> None:
     class EnvBase:
         def __init__(self, device=None, batch_size=None, **k):
             self.device, self.batch_size = device, batch_size
+
+        def set_seed(self, seed=None, static_seed=False):
+            # TorchRL's EnvBase.set_seed hands the seed to the subclass hook
+            self._set_seed(seed)
+            return seed
     envs.EnvBase = EnvBase
     envs.ParallelEnv = object
     data = types.ModuleType("torchrl.data")
     specs = types.ModuleType("torchrl.data.tensor_specs")
-    for nm in ("Composite", "Unbounded", "Categorical"):
+    for nm in ("Composite", "Unbounded", "Categorical", "Bounded"):
         setattr(specs, nm, lambda *a, **k: types.SimpleNamespace(**k))
     mods = {
         "panda3d": panda3d, "panda3d.core": core, "direct": direct, "direct.showbase": sb,

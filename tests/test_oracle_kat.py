@@ -188,3 +188,64 @@ def test_perspective_correct_texture_coordinates(oracle):
     # window depth is the plane's: 0.5 (1 - 2 / z) + 0.5 with z = z0 + (z1 - z0) u
     z = K.PERSP_Z0 + (K.PERSP_Z1 - K.PERSP_Z0) * u
     assert np.allclose(ref["depth"][0][8:24, 8:24], (1.0 - 1.0 / z)[None, :], rtol=0, atol=1e-6)
+
+
+def _jittered_grid(seed: int, cells: int = 4, size: float = 6.0, origin: float = 4.0):
+    """A cells x cells grid of quads (two triangles each, counter-clockwise in
+    GL's y-up window space) whose interior vertices are moved onto pixel
+    centres (offsets of +-0.5 or +-1.5 px), so that each is a centre shared by
+    up to six triangles and many shared edges run exactly through further
+    centres.  Returns screen points [(sx, sy)] and triangles."""
+    rng = np.random.default_rng(seed)
+    n = cells + 1
+    pts = []
+    for j in range(n):
+        for i in range(n):
+            sx, sy = origin + i * size, origin + j * size
+            if 0 < i < cells and 0 < j < cells:
+                sx += rng.integers(-2, 2) + 0.5
+                sy += rng.integers(-2, 2) + 0.5
+            pts.append((sx, sy))
+    tris = []
+    for j in range(cells):
+        for i in range(cells):
+            a, b, c, d = j * n + i, j * n + i + 1, (j + 1) * n + i + 1, (j + 1) * n + i
+            # screen y grows downwards, so (a, d, c) / (a, c, b) wind counter-clockwise with y up
+            tris += [(a, d, c), (a, c, b)] if (i + j) % 2 == 0 else [(a, d, b), (b, d, c)]
+    return pts, tris
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_shared_edges_are_watertight_on_jittered_meshes(oracle, seed):
+    """Every triangle of a jittered grid rendered on its own: no pixel centre
+    is covered twice and every centre strictly inside the grid is covered
+    once, although edges run through centres at arbitrary slopes."""
+    pts, tris = _jittered_grid(seed)
+    count = np.zeros((K.H, K.W), np.int32)
+    for t in tris:
+        p = np.array([pts[v] for v in t])
+        area = (p[1, 0] - p[0, 0]) * (p[2, 1] - p[0, 1]) - (p[2, 0] - p[0, 0]) * (p[1, 1] - p[0, 1])
+        assert area < 0  # front-facing (counter-clockwise with y up)
+        mesh = K.screen_mesh([pts[v] for v in t], [(0, 1, 2)])
+        count += (_render(oracle, K.scene(), [mesh], [K.node(0)])["winner"][0] >= 0).astype(np.int32)
+    assert count.max() == 1
+    # the grid's outer boundary is the square [4, 28]^2: centres strictly inside it are covered
+    c = np.arange(K.W) + 0.5
+    inside = ((c > 4) & (c < 28))[:, None] & ((c > 4) & (c < 28))[None, :]
+    assert np.all(count[inside] == 1)
+    # on the boundary the top-left rule takes the left (x = 4) and top (y = 4) edges only; no centre lies on
+    # them here (centres are at .5), so coverage is exactly the interior
+    assert np.array_equal(count == 1, inside)
+    # the meshes put centres on shared edges and vertices: count them to show the test exercises the tie rule
+    on_edge = set()
+    for t in tris:
+        p = np.array([pts[v] for v in t])
+        for k in range(3):
+            (x0, y0), (x1, y1) = p[k], p[(k + 1) % 3]
+            for y in range(K.H):
+                for x in range(K.W):
+                    px, py = x + 0.5, y + 0.5
+                    cross = (x1 - x0) * (py - y0) - (y1 - y0) * (px - x0)
+                    if cross == 0 and min(x0, x1) <= px <= max(x0, x1) and min(y0, y1) <= py <= max(y0, y1):
+                        on_edge.add((x, y))
+    assert len(on_edge) >= 40

@@ -186,8 +186,11 @@ def as_rgba8(img) -> np.ndarray:
 
 
 def gl_rows(img: np.ndarray) -> np.ndarray:
-    """Image-order RGBA8 -> the kernels' texel layout (row 0 at ``v = 0``)."""
-    return np.ascontiguousarray(img[::-1])
+    """Image-order RGBA8 -> the kernels' texel layout (row 0 at ``v = 0``).
+    Always a fresh array with positive strides: numpy counts a one-row view
+    with a negative row stride as contiguous, which ``torch.from_numpy``
+    rejects."""
+    return img[::-1].copy(order="C")
 
 
 WHITE = np.full((1, 1, 4), 255, dtype=np.uint8)

@@ -238,3 +238,17 @@ def test_oracle_texture_known_answer(oracle):
     top_row = int(np.argmax(keep.any(axis=1)))
     col = int(np.argmax(keep[top_row]))
     assert np.abs(got[top_row, col] - expect8[top_row, col]).max() <= 1
+
+
+def test_one_row_texture_has_positive_strides():
+    """A one-row image flipped to the texel layout must still be a fresh
+    array with positive strides: numpy calls a one-row view with a negative
+    row stride contiguous, and torch.from_numpy rejects it."""
+    import torch
+    import pybatchrender_gb300 as pbr
+    r = pbr.PBRRenderer(num_scenes=2, device="cpu")
+    node = r.add_node("models/box", 1)
+    for img in (np.zeros((1, 2, 4), np.uint8), np.zeros((1, 1, 3), np.uint8), np.zeros((3, 1), np.uint8)):
+        node.set_texture(img)
+        assert all(s > 0 for s in node.texture.strides)
+        assert torch.from_numpy(node.texture).shape[2] == 4

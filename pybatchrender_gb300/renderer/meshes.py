@@ -45,15 +45,17 @@ class Mesh:
     texture: np.ndarray | None = None
 
     def __post_init__(self) -> None:
-        self.positions = np.ascontiguousarray(self.positions, dtype=np.float32).reshape(-1, 3)
-        self.normals = np.ascontiguousarray(self.normals, dtype=np.float32).reshape(-1, 3)
-        self.indices = np.ascontiguousarray(self.indices, dtype=np.int32).reshape(-1, 3)
+        # fresh C-ordered copies: a view that numpy calls contiguous may still carry a negative stride on a
+        # length-1 axis, which torch.from_numpy rejects
+        self.positions = np.array(self.positions, dtype=np.float32, order="C").reshape(-1, 3)
+        self.normals = np.array(self.normals, dtype=np.float32, order="C").reshape(-1, 3)
+        self.indices = np.array(self.indices, dtype=np.int32, order="C").reshape(-1, 3)
         if self.positions.shape != self.normals.shape:
             raise ValueError("positions and normals must have the same shape")
         if self.indices.size and (self.indices.min() < 0 or self.indices.max() >= len(self.positions)):
             raise ValueError("mesh indices out of range")
         if self.uvs is not None:
-            self.uvs = np.ascontiguousarray(self.uvs, dtype=np.float32).reshape(-1, 2)
+            self.uvs = np.array(self.uvs, dtype=np.float32, order="C").reshape(-1, 2)
             if self.uvs.shape[0] != self.positions.shape[0]:
                 raise ValueError("uvs must have one row per vertex")
         tri_n = self.normals[self.indices]  # [nt,3,3]

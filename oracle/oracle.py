@@ -6,6 +6,11 @@ and the timed CPU baseline; the product package never imports this module.
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its
 ``cpu_baseline`` leg and ``--impl reference`` arm) may use it.
 
+Pixel parity against the reference's own (Panda3D/OpenGL) renders is
+unpinned: that path cannot run here.  The stages before rasterisation are
+pinned by fixtures recorded from the reference (``tests/golden/``) and the
+raster rules by analytic known-answer tests.
+
 Scene format (the same fp32 arrays the CUDA kernels read; produced by
 ``PBRRenderer.export_scene()``):
 

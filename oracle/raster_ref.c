@@ -42,6 +42,15 @@
  * texture (linear min/mag filter without mipmaps, repeat wrap): texel
  * centres at (i + 0.5) / w, texel row 0 at v = 0 (the bottom row of the
  * image, Panda3D's image origin), RGBA8 texels read as c / 255.
+ *
+ * Pinning.  Everything before rasterisation (baked vertices, instance
+ * matrices, colours, view-projection matrices, tiles, uniforms) is pinned by
+ * fixtures recorded from the reference's own code (tests/golden/).  The raster
+ * and shading rules are pinned by analytic known-answer tests
+ * (tests/test_oracle_kat.py, tests/test_api_kat_cpu.py).  Pixel parity against
+ * the reference's own renders is UNPINNED: the reference draws through
+ * Panda3D/OpenGL, which cannot run on these machines, and it holds no pixel
+ * fixture of its own.
  */
 #include <math.h>
 #include <tgmath.h> /* sin/cos/sqrt/exp follow REAL: float math in the FP32 build */

@@ -7,7 +7,8 @@ rasterisation: baked vertices, per-instance model matrices and colours,
 per-scene view-projection matrices, tile rectangles, shader uniforms and the
 ``PBRConfig`` resolution bookkeeping.  ``ref_env_dynamics.npz`` records
 trajectories of the reference's CartPole and Steering environments
-(observations, rewards, done flags and step counters) from seeded inputs.  Usage (from the repository root):
+(observations, rewards, done flags and step counters) from seeded inputs, and
+``ref_steering_scene.npz`` the Steering renderer's node buffers and cameras.  Usage (from the repository root):
 
     python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -120,13 +121,55 @@ def steering_trajectory(B: int = 32, T: int = 200) -> dict:
     return rec
 
 
+def steering_scene(B: int = 8, n: int = 20) -> dict:
+    """The reference's SteeringRenderer: build_obstacles on a seeded world,
+    then two _step calls (the second with grace flags set).  Models other
+    than the box load as the stand-in box: the instance matrices, colours
+    and cameras recorded here do not depend on the mesh."""
+    st = sys.modules["pybatchrender.envs.steering"]
+    load_model = stub_panda3d.Loader.loadModel
+
+    def any_model(self, path):
+        try:
+            return load_model(self, path)
+        except FileNotFoundError:
+            return stub_panda3d.NodePath(os.path.basename(str(path)), stub_panda3d._unit_box())
+    stub_panda3d.Loader.loadModel = any_model
+    try:
+        r = st.SteeringRenderer(st.SteeringConfig(num_scenes=B, device="cpu"))
+        g = torch.Generator().manual_seed(13)
+        xs = torch.tensor(r.cfg.obstacle_x_position, dtype=torch.float32)
+        obstacles = torch.zeros(B, n, 4)
+        obstacles[:, :, 0] = xs[torch.randint(0, len(xs), (B, n), generator=g)]
+        obstacles[:, :, 1] = torch.arange(n, dtype=torch.float32) * 12.0 + 6.0
+        obstacles[:, :, 2] = (torch.rand(B, n, generator=g) < 0.3).float()
+        r.build_obstacles(obstacles)
+        rec = {"obstacles": obstacles.numpy()}
+        for step in range(2):
+            state = torch.rand(B, 6, generator=g) * torch.tensor([20.0, 300.0, 100.0, 1.0, 20.0, 300.0]) \
+                - torch.tensor([10.0, 0.0, 0.0, 0.0, 10.0, 0.0])
+            state[:, 3] = (state[:, 3] > 0.5).float() if step else 0.0
+            r._step(state)
+            rec[f"state{step}"] = state.numpy()
+            for name, node in (("player", r.player_node), ("left", r.left_border), ("right", r.right_border),
+                               ("sphere", r.sphere_node)):
+                for k, v in node_record(node, f"s{step}_{name}").items():
+                    if not k.endswith("_verts"):
+                        rec[k] = v
+            rec.update({f"s{step}_{k}": v for k, v in camera_record(r._pbr_cam, B).items()})
+    finally:
+        stub_panda3d.Loader.loadModel = load_model
+    return rec
+
+
 def main(ref_path: str) -> None:
     pbr, cp = import_reference(ref_path)
     with contextlib.redirect_stdout(io.StringIO()):
         import pybatchrender.envs.steering  # noqa: F401
         rec = cartpole_trajectory(cp)
         rec.update(steering_trajectory())
-    np.savez_compressed(os.path.join(HERE, "ref_env_dynamics.npz"), **rec)
+        np.savez_compressed(os.path.join(HERE, "ref_env_dynamics.npz"), **rec)
+        np.savez_compressed(os.path.join(HERE, "ref_steering_scene.npz"), **steering_scene())
     with contextlib.redirect_stdout(io.StringIO()):
         for N, keep in ((5, None), (64, None), (4098, 16)):
             r = cp.CartPoleRenderer(cp.CartPoleConfig(num_scenes=N))

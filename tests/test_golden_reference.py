@@ -105,3 +105,38 @@ def test_api_scene_oracle_matrices_match_reference():
     for name, node in zip("abc", r.nodes_abc):
         got = oracle.instance_matrices(dict(node.export(), mesh=0))
         assert np.allclose(got, ref[f"{name}_M"], rtol=1e-5, atol=1e-6), name
+
+
+def test_steering_scene_matches_reference():
+    """Steering-v0's renderer against the reference's: obstacle spheres
+    (positions, red/gold colours), the player (position, crash colour during
+    the grace period), the rails and the camera that follows the player, over
+    build_obstacles and two _step calls."""
+    from pybatchrender_gb300.envs.steering import SteeringConfig, SteeringRenderer
+    ref = load("ref_steering_scene.npz")
+    B = ref["state0"].shape[0]
+    r = SteeringRenderer(SteeringConfig(num_scenes=B, device="cpu"))
+    r.build_obstacles(torch.from_numpy(ref["obstacles"]))
+    for step in range(2):
+        state = ref[f"state{step}"]
+        r._step(torch.from_numpy(state))
+        for name, node in (("player", r.player_node), ("sphere", r.sphere_node)):
+            assert np.allclose(node.get_transforms().numpy(), ref[f"s{step}_{name}_M"], rtol=1e-6, atol=1e-6), name
+            assert np.array_equal(node.color.numpy(), ref[f"s{step}_{name}_color"]), name
+        for name, node in (("left", r.left_border), ("right", r.right_border)):
+            got, want = node.get_transforms().numpy(), ref[f"s{step}_{name}_M"]
+            assert np.array_equal(node.color.numpy(), ref[f"s{step}_{name}_color"]), name
+            # the reference moves the rails with set_positions(..., lazy=True), which it never uploads, so its
+            # rails stay at y = 0; here a lazy update is current at the next render and the rails follow the
+            # player (the reference's evident intent, envs/steering/renderer.py:262-265)
+            assert np.all(want[:, 1, 3] == 0.0) and np.allclose(got[:, 1, 3], state[:, 1]), name
+            got[:, 1, 3] = 0.0
+            assert np.allclose(got, want, rtol=1e-6, atol=1e-6), name
+        assert np.allclose(r._pbr_cam.VP_k44.numpy(), ref[f"s{step}_VP"], rtol=1e-5, atol=1e-5)
+        assert np.allclose(r._pbr_cam.P_k44.numpy(), ref[f"s{step}_P"], rtol=1e-7, atol=0)
+        assert np.array_equal(r._pbr_cam.tiles_k4.numpy(), ref[f"s{step}_tiles"])
+    light = r._pbr_light
+    assert np.allclose(ref["s1_player_in_dirLightDir"], light.dir_dir)
+    assert np.allclose(ref["s1_player_in_ambientCol"], light.ambient)
+    assert np.allclose(ref["s1_player_in_dirLightCol"], light.dir_col)
+    assert (ref["state1"][:, 3] > 0.5).any() and (ref["state1"][:, 3] < 0.5).any()  # both player colours occur

@@ -8,7 +8,8 @@ per-scene view-projection matrices, tile rectangles, shader uniforms and the
 ``PBRConfig`` resolution bookkeeping.  ``ref_env_dynamics.npz`` records
 trajectories of the reference's CartPole and Steering environments
 (observations, rewards, done flags and step counters) from seeded inputs, and
-``ref_steering_scene.npz`` the Steering renderer's node buffers and cameras.  Usage (from the repository root):
+``ref_steering_scene.npz`` the Steering renderer's node buffers and cameras;
+``ref_config_defaults.json`` holds the default of every configuration field.  Usage (from the repository root):
 
     python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -53,6 +54,14 @@ def node_record(node, prefix: str) -> dict:
 def camera_record(cam, N: int) -> dict:
     vp = cam.viewbuf.array((N, 4, 4)).transpose(0, 2, 1)
     return {"VP": vp, "tiles": cam.tilebuf.array((N, 4)), "P": cam.P_k44.numpy()}
+
+
+def _jsonable(v):
+    if isinstance(v, (tuple, list)):
+        return [_jsonable(x) for x in v]
+    if isinstance(v, (bool, int, float, str)) or v is None:
+        return v
+    return repr(v)
 
 
 def cartpole_trajectory(cp, B: int = 64, T: int = 60) -> dict:
@@ -199,6 +208,15 @@ def main(ref_path: str) -> None:
         light = r._pbr_light
         rec["light"] = np.asarray(light.ambient + light.dir_dir + light.dir_col + (light.strength,), np.float64)
         np.savez_compressed(os.path.join(HERE, "ref_api_scene.npz"), **rec)
+
+    defaults = {}
+    import dataclasses
+    import pybatchrender.envs.steering as st
+    for name, cls in (("PBRConfig", pbr.PBRConfig), ("CartPoleConfig", cp.CartPoleConfig),
+                      ("SteeringConfig", st.SteeringConfig)):
+        defaults[name] = {f.name: _jsonable(getattr(cls(device="cpu"), f.name)) for f in dataclasses.fields(cls)}
+    with open(os.path.join(HERE, "ref_config_defaults.json"), "w") as f:
+        json.dump(defaults, f, indent=1, sort_keys=True)
 
     cases = []
     for kw in scenes.CONFIG_CASES:

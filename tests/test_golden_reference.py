@@ -140,3 +140,36 @@ def test_steering_scene_matches_reference():
     assert np.allclose(ref["s1_player_in_ambientCol"], light.ambient)
     assert np.allclose(ref["s1_player_in_dirLightCol"], light.dir_col)
     assert (ref["state1"][:, 3] > 0.5).any() and (ref["state1"][:, 3] < 0.5).any()  # both player colours occur
+
+
+def _jsonable(v):
+    if isinstance(v, (tuple, list)):
+        return [_jsonable(x) for x in v]
+    if isinstance(v, (bool, int, float, str)) or v is None:
+        return v
+    return repr(v)
+
+
+def test_config_defaults_match_reference():
+    """Every field of the reference's PBRConfig, CartPoleConfig and
+    SteeringConfig exists here with the same default; the only difference is
+    Steering's rail model (the reference's glTF file is not part of this
+    package: the procedural cylinder stands in).  The extra fields are this
+    renderer's own options."""
+    import dataclasses
+    from pybatchrender_gb300.envs.cartpole import CartPoleConfig
+    from pybatchrender_gb300.envs.steering import SteeringConfig
+    ref = json.load(open(os.path.join(GOLDEN, "ref_config_defaults.json")))
+    allowed = {("SteeringConfig", "border_model"): ("models/cylinder/scene.gltf", "models/cylinder")}
+    own = {"autotune", "bin_size", "cuda_graph", "fused_step", "persistent", "raster_kernel", "raster_method",
+           "raster_mode", "raster_threads", "return_depth", "reuse_output", "soft_gamma", "soft_sigma", "tri_cap"}
+    for name, cls in (("PBRConfig", pbr.PBRConfig), ("CartPoleConfig", CartPoleConfig),
+                      ("SteeringConfig", SteeringConfig)):
+        ours = {f.name: _jsonable(getattr(cls(device="cpu"), f.name)) for f in dataclasses.fields(cls)}
+        assert set(ref[name]) <= set(ours), (name, set(ref[name]) - set(ours))
+        assert set(ours) - set(ref[name]) <= own, (name, set(ours) - set(ref[name]) - own)
+        for k, v in ref[name].items():
+            if (name, k) in allowed:
+                assert (v, ours[k]) == allowed[(name, k)]
+            else:
+                assert ours[k] == v, (name, k, v, ours[k])

@@ -9,7 +9,8 @@ per-scene view-projection matrices, tile rectangles, shader uniforms and the
 trajectories of the reference's CartPole and Steering environments
 (observations, rewards, done flags and step counters) from seeded inputs, and
 ``ref_steering_scene.npz`` the Steering renderer's node buffers and cameras;
-``ref_config_defaults.json`` holds the default of every configuration field.  Usage (from the repository root):
+``ref_config_defaults.json`` holds the default of every configuration field
+and ``ref_grid_frames.npz`` the snapshot grids of ``PBREnv._make_grid_frame``.  Usage (from the repository root):
 
     python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -171,8 +172,33 @@ def steering_scene(B: int = 8, n: int = 20) -> dict:
     return rec
 
 
+GRID_CASES = [  # (pixel batch shape, float pixels, indices, num)
+    ((7, 3, 5, 4), False, None, 16),
+    ((9, 3, 4, 6), False, [6, -1, 2, 100, 0], 3),
+    ((5, 1, 3, 3), True, None, 4),
+    ((2, 3, 3, 4, 4), False, [5, 1], 16),
+    ((3, 4, 2, 2), False, None, 0),
+]
+
+
+def grid_frames(env_cls) -> dict:
+    """The reference's PBREnv._make_grid_frame (scale 1: no PIL involved) on
+    seeded pixel batches of GRID_CASES."""
+    g = torch.Generator().manual_seed(14)
+    rec = {}
+    for i, (shape, as_float, indices, num) in enumerate(GRID_CASES):
+        if as_float:
+            pix = torch.rand(shape, generator=g) * 400.0 - 50.0
+        else:
+            pix = torch.randint(0, 256, shape, generator=g, dtype=torch.uint8)
+        rec[f"pixels{i}"] = pix.numpy()
+        rec[f"grid{i}"] = env_cls._make_grid_frame(None, pix, indices, num, 1)
+    return rec
+
+
 def main(ref_path: str) -> None:
     pbr, cp = import_reference(ref_path)
+    np.savez_compressed(os.path.join(HERE, "ref_grid_frames.npz"), **grid_frames(pbr.PBREnv))
     with contextlib.redirect_stdout(io.StringIO()):
         import pybatchrender.envs.steering  # noqa: F401
         rec = cartpole_trajectory(cp)

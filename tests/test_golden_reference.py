@@ -173,3 +173,18 @@ def test_config_defaults_match_reference():
                 assert (v, ours[k]) == allowed[(name, k)]
             else:
                 assert ours[k] == v, (name, k, v, ours[k])
+
+
+def test_grid_frames_match_reference():
+    """save_batch_examples / save_batch_gif grids against the reference's
+    _make_grid_frame: layout (rows = ceil(sqrt(k))), index filtering, 5-D
+    batches, float clamping and the k >= 1 rule; the 2x nearest upscale is
+    pixel replication."""
+    from pybatchrender_gb300.imagefile import make_grid
+    ref = load("ref_grid_frames.npz")
+    cases = [(None, 16), ([6, -1, 2, 100, 0], 3), (None, 4), ([5, 1], 16), (None, 0)]
+    for i, (indices, num) in enumerate(cases):
+        got = make_grid(torch.from_numpy(ref[f"pixels{i}"]), indices, num, 1)
+        assert got.dtype == np.uint8 and np.array_equal(got, ref[f"grid{i}"]), i
+    big = make_grid(torch.from_numpy(ref["pixels0"]), None, 16, 2)
+    assert np.array_equal(big, ref["grid0"].repeat(2, axis=0).repeat(2, axis=1))

@@ -46,3 +46,20 @@ def test_fp32_baseline_known_answers(oracle):
     for c in range(3):
         assert np.all(got["pixels"][0][c][cov] == K.FACE_EXPECT[c])
     assert np.all(got["depth"][0][cov] == 0.625)
+
+
+@pytest.mark.parametrize("workload", ["many_cubes", "uneven"])
+def test_fp32_baseline_matches_fp64_on_other_workloads(oracle, workload):
+    from pybatchrender_gb300 import workloads
+    if workload == "many_cubes":
+        r = workloads.many_cubes(num_scenes=8, res=64, instances=16, device="cpu")
+    else:
+        r = workloads.uneven(num_scenes=8, res=48, max_instances=24, device="cpu")
+    sc, me, no = r.export_scene()
+    ref = oracle.render_hard(sc, me, no, want_winner=True, want_ambiguous=True)
+    got = oracle.render_hard(sc, me, no, want_winner=True, precision="f32", nthreads=3)
+    ok = ~ref["ambiguous"]
+    assert np.array_equal(got["winner"][ok], ref["winner"][ok])
+    diff = np.abs(got["pixels"].astype(np.int16) - ref["pixels"].astype(np.int16)).max(axis=1)
+    assert diff[ok].max(initial=0) <= 1
+    assert (ref["winner"] >= 0).sum() > 100

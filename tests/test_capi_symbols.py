@@ -76,3 +76,45 @@ def test_cartpole_step_argument_checks_without_gpu(lib):
     bad = list(args)
     bad[1] = None
     assert f(*bad, 8, consts, 0, None) == _capi.PBR_ERR_INVALID
+
+
+_NULL_CTX_PROBE = r"""
+import ctypes, sys
+from pybatchrender_gb300 import _capi
+from pybatchrender_gb300.build import LIB_PATH
+lib = ctypes.CDLL(LIB_PATH)
+lib.pbr_last_error.restype = ctypes.c_char_p
+lib.pbr_last_error.argtypes = [ctypes.c_void_p]
+bad = []
+for name, sig in _capi.SIGNATURES.items():
+    if not sig or sig[0] is not ctypes.c_void_p or name in ("pbr_destroy", "pbr_cartpole_step"):
+        continue
+    args = []
+    for t in sig:
+        if t in (ctypes.c_int, ctypes.c_long, ctypes.c_longlong):
+            args.append(0)
+        elif t in (ctypes.c_float, ctypes.c_double):
+            args.append(0.0)
+        elif isinstance(t, type) and issubclass(t, ctypes.Array):
+            args.append(t())
+        else:
+            args.append(None)
+    f = getattr(lib, name)
+    f.argtypes, f.restype = sig, ctypes.c_int
+    rc = f(*args)
+    if rc != _capi.PBR_ERR_INVALID or lib.pbr_last_error(None) != b"null context":
+        bad.append((name, rc))
+print("checked", len([n for n in _capi.SIGNATURES]), "bad", bad)
+sys.exit(1 if bad else 0)
+"""
+
+
+def test_every_context_call_rejects_a_null_context(lib):
+    """Each entry point that takes a context returns PBR_ERR_INVALID for a
+    null one before touching anything (run in a child process, so that a
+    missing check cannot take the test session down)."""
+    import subprocess
+    import sys
+    res = subprocess.run([sys.executable, "-c", _NULL_CTX_PROBE], cwd=ROOT, capture_output=True, text=True,
+                         timeout=120)
+    assert res.returncode == 0, res.stdout + res.stderr

@@ -17,6 +17,7 @@ import json
 import math
 import os
 import struct
+import zlib
 from collections.abc import Sequence
 from dataclasses import dataclass, field
 
@@ -258,7 +259,11 @@ def load_egg(path: str) -> Mesh:
     texture."""
     from .textures import load_image
 
-    items, _ = _egg_parse(_egg_tokens(open(path, "r", encoding="utf-8").read()))
+    with open(path, "rb") as f:
+        raw = f.read()
+    if path.lower().endswith(".pz"):
+        raw = zlib.decompress(raw)  # Panda3D's pzip: one zlib stream
+    items, _ = _egg_parse(_egg_tokens(raw.decode("utf-8")))
     cs = "z-up"
     for e in _egg_entries(items, "CoordinateSystem"):
         cs = " ".join(_egg_values(e[2])).lower()
@@ -537,21 +542,31 @@ _BUILTIN = {
 }
 
 
+_MODEL_EXTENSIONS = (".egg", ".egg.pz", ".gltf", ".glb")
+
+
 def resolve_model(model: "str | Mesh") -> Mesh:
     """Map a reference-style model path to a mesh.
 
     ``"models/box"`` / ``"box"`` -> :func:`unit_cube` (Panda3D's bundled box);
     ``"cylinder"``, ``"cylinder:<segments>"``, ``"icosphere:<level>"`` ->
-    procedural shapes; an existing ``.egg`` / ``.gltf`` file -> the loaders
-    above.  A :class:`Mesh` is returned as a copy.
+    procedural shapes; an existing ``.egg`` / ``.egg.pz`` / ``.gltf`` / ``.glb``
+    file (the extension may be left out, as with Panda3D's loader) -> the
+    loaders above.  A :class:`Mesh` is returned as a copy.
     """
     if isinstance(model, Mesh):
         return model.copy()
     if not isinstance(model, str):
         raise TypeError(f"model_path must be a str or Mesh, got {type(model).__name__}")
+    if not os.path.isfile(model):
+        # like Panda3D's loader, a path without an extension finds the file with one
+        for ext in _MODEL_EXTENSIONS:
+            if os.path.isfile(model + ext):
+                model = model + ext
+                break
     if os.path.isfile(model):
         low = model.lower()
-        if low.endswith(".egg"):
+        if low.endswith(".egg") or low.endswith(".egg.pz"):
             return load_egg(model)
         if low.endswith(".gltf") or low.endswith(".glb"):
             return load_gltf(model)

@@ -118,6 +118,22 @@ def test_egg_pools_groups_and_axes(tmp_path):
         meshes.resolve_model(str(tmp_path / "bad.egg"))
 
 
+def test_egg_pz_and_paths_without_extension(tmp_path):
+    """Panda3D's compressed ``.egg.pz`` (one zlib stream) loads like the
+    plain file, and a path without an extension finds the file with one."""
+    import zlib
+    (tmp_path / "plain.egg").write_text(EGG % "Z-Up")
+    (tmp_path / "packed.egg.pz").write_bytes(zlib.compress((EGG % "Z-Up").encode()))
+    a = meshes.resolve_model(str(tmp_path / "plain.egg"))
+    b = meshes.resolve_model(str(tmp_path / "packed.egg.pz"))
+    c = meshes.resolve_model(str(tmp_path / "plain"))
+    d = meshes.resolve_model(str(tmp_path / "packed"))
+    for m in (b, c, d):
+        assert np.array_equal(m.positions, a.positions) and np.array_equal(m.indices, a.indices)
+    with pytest.raises(FileNotFoundError):
+        meshes.resolve_model(str(tmp_path / "missing"))
+
+
 def test_gltf_normalized_texcoords(tmp_path):
     doc, blob = _doc("tri.bin")
     uv16 = np.array([[0, 0], [65535, 0], [0, 32768]], np.uint16)

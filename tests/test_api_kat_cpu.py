@@ -83,3 +83,45 @@ def test_turned_cube_shows_two_faces_lit_at_45_degrees(oracle, cubes):
     # the turned cube is wider than the front face alone: its silhouette spans the diagonal 0.5 * sqrt(2)
     cols = np.nonzero(cov.any(axis=0))[0]
     assert cols.max() - cols.min() + 1 > 12
+
+
+def _floor_coverage(ndc_x, ndc_y, t, aspect, X, Y):
+    """Analytic coverage of the floor quad |x| <= X, |y| <= Y, z = -1 seen
+    from the origin looking along +y (up +z): the pixel ray
+    d = (ndc_x t aspect, 1, ndc_y t) hits the floor at s = -1 / d_z."""
+    dz = ndc_y * t
+    with np.errstate(divide="ignore", invalid="ignore"):
+        s = np.where(dz < 0, -1.0 / dz, np.inf)
+    hx, hy = s * ndc_x * t * aspect, s
+    return (dz < 0) & (np.abs(hx) <= X) & (hy <= Y)
+
+
+def test_floor_through_the_near_plane(oracle):
+    """A floor quad that reaches 20 units behind the camera (its far half is
+    behind the eye, w < 0): near-plane clipping keeps exactly the pixels
+    whose rays hit the quad in front of the camera; without clipping the
+    vertices behind the eye would project to the wrong side of the image."""
+    from pybatchrender_gb300.renderer.meshes import Mesh
+    X, Y, res = 3.0, 20.0, 64
+    r = pbr.PBRRenderer(num_scenes=1, tile_resolution=(res, res), device="cpu")
+    pts = np.array([(-X, -Y, -1.0), (X, -Y, -1.0), (X, Y, -1.0), (-X, Y, -1.0)], np.float32)
+    floor = r.add_node(Mesh(pts, np.tile([0.0, 0.0, 1.0], (4, 1)), [(0, 1, 2), (0, 2, 3)], name="floor"), 1)
+    floor.set_colors(torch.tensor([[0.4, 0.6, 0.8, 1.0]]))
+    cam = r.add_camera(fov_y_deg=60.0, z_near=0.05, z_far=100.0)
+    cam.set_positions_and_lookat(torch.tensor([0.0, 0.0, 0.0]), torch.tensor([0.0, 1.0, 0.0]))
+    r.add_light(strength=0.0)
+    r.setup_environment()
+    ref = oracle.render_hard(*r.export_scene(), want_winner=True, want_ambiguous=True)
+    cov = ref["winner"][0] >= 0
+    c = (np.arange(res) + 0.5) / res * 2 - 1
+    nx, ny = c[None, :], -c[:, None]
+    t = math.tan(math.radians(30.0))
+    expect = _floor_coverage(nx, ny, t, 1.0, X, Y)
+    # centres within 1e-3 px of the quad's outline are left out (the rule there is the fill rule's, tested elsewhere)
+    e = 2e-3 / res
+    stable = np.ones_like(expect)
+    for dx, dy in ((e, 0), (-e, 0), (0, e), (0, -e)):
+        stable &= _floor_coverage(nx + dx, ny + dy, t, 1.0, X, Y) == expect
+    assert stable.mean() > 0.95
+    assert np.array_equal(cov[stable], expect[stable])
+    assert expect.sum() > 500 and not cov[: res // 2].any()  # the whole upper half (above the horizon) is empty

@@ -10,7 +10,9 @@ trajectories of the reference's CartPole and Steering environments
 (observations, rewards, done flags and step counters) from seeded inputs, and
 ``ref_steering_scene.npz`` the Steering renderer's node buffers and cameras;
 ``ref_config_defaults.json`` holds the default of every configuration field
-and ``ref_grid_frames.npz`` the snapshot grids of ``PBREnv._make_grid_frame``.  Usage (from the repository root):
+``ref_grid_frames.npz`` the snapshot grids of ``PBREnv._make_grid_frame`` and
+``ref_defaults_scene.npz`` a scene built with every node, camera and light
+argument left at its default.  Usage (from the repository root):
 
     python tests/golden/make_golden.py [/path/to/reference]
 """
@@ -234,6 +236,15 @@ def main(ref_path: str) -> None:
         light = r._pbr_light
         rec["light"] = np.asarray(light.ambient + light.dir_dir + light.dir_col + (light.strength,), np.float64)
         np.savez_compressed(os.path.join(HERE, "ref_api_scene.npz"), **rec)
+
+        d = scenes.defaults_scene(pbr)
+        rec = node_record(d.box, "box")
+        rec.update(camera_record(d._pbr_cam, d.num_scenes))
+        light = d._pbr_light
+        rec["light"] = np.asarray(light.ambient + light.dir_dir + light.dir_col + (light.strength,), np.float64)
+        cam = d._pbr_cam
+        rec["cam_params"] = np.asarray([cam.fov_y_deg, cam.z_near, cam.z_far], np.float64)
+        np.savez_compressed(os.path.join(HERE, "ref_defaults_scene.npz"), **rec)
 
     defaults = {}
     import dataclasses

@@ -74,6 +74,21 @@ def api_scene(pbr, num_scenes: int = 6, **cfg):
     return r, snaps
 
 
+def defaults_scene(pbr, num_scenes: int = 3, **cfg):
+    """add_node / add_camera / add_light with every argument left at its
+    default (the box at the origin, the default eye and light)."""
+
+    class Scene(pbr.PBRRenderer):
+        def __init__(self):
+            super().__init__(num_scenes=num_scenes, tile_resolution=(40, 24), **cfg)
+            self.box = self.add_node("models/box", 1)
+            self.add_camera()
+            self.light = self.add_light()
+            self.setup_environment()
+
+    return Scene()
+
+
 def cartpole_states(n: int, seed: int) -> torch.Tensor:
     g = torch.Generator().manual_seed(seed)
     st = torch.zeros((n, 4))

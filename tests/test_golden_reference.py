@@ -188,3 +188,23 @@ def test_grid_frames_match_reference():
         assert got.dtype == np.uint8 and np.array_equal(got, ref[f"grid{i}"]), i
     big = make_grid(torch.from_numpy(ref["pixels0"]), None, 16, 2)
     assert np.array_equal(big, ref["grid0"].repeat(2, axis=0).repeat(2, axis=1))
+
+
+def test_defaults_scene_matches_reference():
+    """add_node / add_camera / add_light with default arguments: the default
+    instance (identity at the origin, white), the default eye and projection
+    (fov 55 degrees, near 0.05, far 100, aspect of the whole window) and the
+    default light, as the reference builds them."""
+    ref = load("ref_defaults_scene.npz")
+    r = scenes.defaults_scene(pbr, device="cpu")
+    assert np.allclose(r.box.get_transforms().numpy(), ref["box_M"], rtol=0, atol=1e-7)
+    assert np.array_equal(r.box.color.numpy(), ref["box_color"])
+    assert np.allclose(sorted_rows(r.box.mesh.positions), sorted_rows(ref["box_verts"]), atol=1e-6)
+    cam = r._pbr_cam
+    assert np.allclose([cam.fov_y_deg, cam.z_near, cam.z_far], ref["cam_params"])
+    assert np.allclose(cam.P_k44.numpy(), ref["P"], rtol=1e-7, atol=0)
+    assert np.allclose(cam.VP_k44.numpy(), ref["VP"], rtol=1e-6, atol=1e-6)
+    assert np.array_equal(cam.tiles_k4.numpy(), ref["tiles"])
+    light = r._pbr_light
+    assert np.allclose(ref["light"], light.ambient + light.dir_dir + light.dir_col + (light.strength,))
+    assert tuple(ref["box_in_screenSize"]) == tuple(float(v) for v in r.cfg.window_resolution)

@@ -16,7 +16,9 @@
  * Conventions
  *  - Every entry point returns an int status: PBR_OK (0) or a PBR_ERR_* code.
  *    pbr_last_error() returns a message for the last failing call on a context
- *    (or, with ctx == NULL, for the last failing pbr_create on this thread).
+ *    (or, with ctx == NULL, for the last failing pbr_create, or call given a
+ *    null context, on this thread).  pbr_cartpole_step takes no context and
+ *    reports through its status alone.
  *  - Pointers named d_* are device pointers on the context's device.  They are
  *    borrowed, never freed: the caller keeps them alive while they are bound.
  *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default

@@ -73,6 +73,7 @@ typedef REAL real;
 
 #define SOFT_CUTOFF 16.0  /* soft coverage is 0 beyond 16 sigma outside an edge */
 #define SOFT_TAPER 4.0    /* tapered to 0 over the last 4 sigma */
+#define SOFT_DEPTH_SAT 0.125 /* saturation depth of the extended plane, in units of zfar - znear */
 
 #define ORC_MODE_HPR 0
 #define ORC_MODE_ROT 1
@@ -591,7 +592,11 @@ int FN(orc_instance_matrices)(const orc_node* nd, int64_t B, float* out) {
  *           from p to the triangle (0 inside), T(d) = S((16 sigma - d) / (4 sigma)),
  *           S(x) = x^3 (6x^2 - 15x + 10) on [0,1], 0 below, 1 above: exactly 0 once
  *           p is 16 sigma or more away from the triangle
- *   1/w   = sum_k b_k / w_k                    b_k = E_k / area2 (unclamped)
+ *   1/x   = sum_k b_k / w_k                    b_k = E_k / area2 (unclamped): the depth x
+ *           of the triangle's plane; w = x up to w_hi = max_k w_k, w = w_hi + s (1 - exp(-(x -
+ *           w_hi) / s)) beyond it with s = (zfar - znear) / 8, and w = w_hi + s where
+ *           sum_k b_k / w_k <= 0: the extended plane's depth stays bounded and smooth instead of
+ *           running off to infinity near the vanishing line of a face seen nearly edge-on
  *   zs_j  = (zfar - w) / (zfar - znear)        normalised linear depth, nearer = larger
  *   C_j   = basic.frag shading with the perspective-correct (extrapolated) normal,
  *           unclamped
@@ -682,11 +687,22 @@ static void soft_cb(void* user, const stri* t, const real col[4], int32_t wid) {
             real b0 = E[0] / t->area2, b1 = E[1] / t->area2, b2 = E[2] / t->area2;
             real q0 = b0 * t->iw[0], q1 = b1 * t->iw[1], q2 = b2 * t->iw[2];
             real qs = q0 + q1 + q2;
-            if (!(qs > 0)) continue;
-            real w = (real)1 / qs;
+            real whi = (real)1 / t->iw[0];
+            for (int k = 1; k < 3; ++k) {
+                real wk = (real)1 / t->iw[k];
+                if (wk > whi) whi = wk;
+            }
+            real sat = (real)SOFT_DEPTH_SAT * ((real)sc->zfar - (real)sc->znear);
+            real w = whi + sat;
+            if (qs > 0) {
+                w = (real)1 / qs;
+                if (w > whi) w = whi + sat * (1 - exp(-(w - whi) / sat));
+            }
             real zs = ((real)sc->zfar - w) / ((real)sc->zfar - (real)sc->znear);
             real nn[3], C[4];
-            for (int c = 0; c < 3; ++c) nn[c] = (q0 * t->n[0][c] + q1 * t->n[1][c] + q2 * t->n[2][c]) * w;
+            /* perspective-correct normal, oriented by the sign of the interpolation denominator */
+            real orient = qs < 0 ? (real)-1 : (real)1;
+            for (int c = 0; c < 3; ++c) nn[c] = (q0 * t->n[0][c] + q1 * t->n[1][c] + q2 * t->n[2][c]) * orient;
             shade(sc, s->Ln, nn, col, C);
             int64_t o = (int64_t)y * sc->W + x;
             s->Pi[o] *= (1 - D);

@@ -8,7 +8,9 @@ torch autograd gives the reference gradients.  The model is the one of
 (``renderer/shader_context.py:47-84``), GL viewport into the scene's own
 image, back faces culled, triangles not fully in front of the near plane
 dropped, coverage ``D = prod_k sigmoid(e_k/sigma) T(d)`` with the C2 taper of the
-distance ``d`` from the pixel to the triangle,
+distance ``d`` from the pixel to the triangle, the triangle's plane depth at the
+pixel saturating smoothly beyond the triangle's farthest vertex depth (and
+beyond the plane's vanishing line),
 normalised linear depth, shading of ``shaders/basic.frag:33-38`` (unclamped),
 softmax depth blend and alpha composite over the background.
 
@@ -23,6 +25,7 @@ import torch
 
 CUT = 16.0
 TAPER = 4.0
+DEPTH_SAT = 0.125  # saturation depth of the extended plane, in units of zfar - znear
 
 
 def params_from_nodes(nodes: list, requires_grad: bool = True) -> list[dict]:
@@ -136,14 +139,22 @@ def render(scene: dict, meshes: list, nodes: list, params: list[dict], light_dir
         dout = torch.where(emin0 < 0, torch.minimum(torch.minimum(dseg[0], dseg[1]), dseg[2]), torch.zeros_like(emin0))
         D = fk[0] * fk[1] * fk[2] * _taper(dout, sigma)
         Q = E[0] * iw[:, 0, None] + E[1] * iw[:, 1, None] + E[2] * iw[:, 2, None]
-        emin = torch.minimum(torch.minimum(e[0], e[1]), e[2])
-        valid = ((emin > -CUT * sigma) & (Q > 0) & (D > 0)).detach()
-        Qs = torch.where(valid, Q, torch.ones_like(Q))
-        w = area2[:, None] / Qs
+        qpos = (Q > 0).detach()
+        Qs = torch.where(qpos, Q, torch.ones_like(Q))
+        wv = 1.0 / iw  # vertex clip w [T,3]
+        whi = torch.maximum(torch.maximum(wv[:, 0], wv[:, 1]), wv[:, 2])[:, None].expand_as(Q)
+        sat = DEPTH_SAT * (zf - zn)
+        w_raw = area2[:, None] / Qs
+        beyond = (w_raw > whi).detach()
+        w_sat = whi + sat * (1 - torch.exp(-torch.where(beyond, w_raw - whi, torch.zeros_like(w_raw)) / sat))
+        w = torch.where(~qpos, whi + sat, torch.where(beyond, w_sat, w_raw))
         zs = (zf - w) / (zf - zn)
+        emin = torch.minimum(torch.minimum(e[0], e[1]), e[2])
+        valid = ((emin > -CUT * sigma) & (D > 0)).detach()
         # shading
-        u_s = (E[0] * iw[:, 0, None])[..., None] * n[:, None, 0] + (E[1] * iw[:, 1, None])[..., None] * n[:, None, 1] \
-            + (E[2] * iw[:, 2, None])[..., None] * n[:, None, 2]
+        orient = torch.where(Q < 0, -1.0, 1.0).detach()[..., None]
+        u_s = ((E[0] * iw[:, 0, None])[..., None] * n[:, None, 0] + (E[1] * iw[:, 1, None])[..., None] * n[:, None, 1]
+               + (E[2] * iw[:, 2, None])[..., None] * n[:, None, 2]) * orient
         u_f = n[:, None, 0].expand_as(u_s)
         u = torch.where(sm[:, None, None], u_s, u_f)
         ulen = torch.linalg.norm(torch.where(valid[..., None], u, torch.ones_like(u)), dim=-1)

@@ -8,7 +8,13 @@
 //   e_k  = E_k(p) / |(A_k, B_k)|            signed distance to edge line k (px)
 //   D_j  = prod_k sigmoid(e_k / sigma) T(d),  d = distance from p to the triangle (0 inside),
 //          T = smootherstep((16 sigma - d) / (4 sigma)): C1 everywhere, exactly 0 at 16 sigma
-//   w    = area2 / sum_k E_k iw_k           perspective-correct clip w
+//   w    = sat(area2 / Q),  Q = sum_k E_k iw_k: the perspective-correct clip w of the triangle's
+//          plane; sat(x) = x up to the triangle's farthest vertex depth w_hi = max_k w_k, and
+//          w_hi + s (1 - exp(-(x - w_hi) / s)) beyond it, s = (zfar - znear) / 8; w_hi + s where
+//          Q <= 0.  Inside the triangle nothing changes; outside, the extended plane's depth would
+//          run off to infinity near the vanishing line of a face seen nearly edge-on (Q changes sign
+//          there, inside the soft footprint), and sat keeps it bounded and smooth in the pose (C1
+//          at w_hi, C-infinity across Q = 0)
 //   zs_j = (zfar - w) / (zfar - znear)      nearer = larger
 //   C_j  = shading of shaders/basic.frag:33-38 (unclamped) with the
 //          perspective-correct normal
@@ -30,6 +36,7 @@ namespace pbr {
 
 constexpr float kSoftCut = 16.f;    // coverage is 0 at 16 sigma or more from the triangle
 constexpr float kSoftTaper = 4.f;   // tapered to 0 over the last 4 sigma
+constexpr float kSoftDepthSat = 0.125f;  // saturation depth s of the extended plane, / (zfar - znear)
 constexpr int kSoftRecs = 15;
 constexpr int kIacc = 24; // per-instance gradient accumulator: dM3 (9), dt (3), dcol (3), dM3 normal chain (9)
 
@@ -112,9 +119,12 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // Fragment of chunk triangle t at pixel centre (px, py).  Returns false when
-// the pixel is beyond the cutoff or behind the eye.
+// the pixel is beyond the cutoff.
 struct Frag {
   float E[3], e[3], sg[3], D, Ds, dTdd, Q, w, zs;  // sg = sigmoid per edge, Ds = prod sg, D = Ds * T(d)
+  float qsgn;                                       // sign of Q (orients the interpolated normal)
+  float zsat;                                       // d sat / dx where saturated (0 where Q <= 0)
+  int zk;                                           // saturated beyond vertex zk's depth (-1: not)
   int seg_a, seg_b;                                 // closest segment (vertex indices) when T' != 0
   float seg_t, ux, uy;                              // its parameter and the unit vector from it to p
   float C[3], l[3], ndl, un[3], ulen;  // shaded colour, light factor, normal (u = unnormalised)
@@ -132,7 +142,7 @@ __device__ __forceinline__ bool soft_frag(const SceneParams& P, const SoftCtx& S
   const float emin = fminf(fminf(f.e[0], f.e[1]), f.e[2]);
   if (!(emin > -S.cut)) return false;
   f.Q = f.E[0] * iw.x + f.E[1] * iw.y + f.E[2] * iw.z;
-  if (!(f.Q > 0.f)) return false;
+  f.qsgn = f.Q < 0.f ? -1.f : 1.f;
 #pragma unroll
   for (int k = 0; k < 3; ++k) f.sg[k] = 1.f / (1.f + expf(-f.e[k] * inv_sigma));
   f.Ds = f.sg[0] * f.sg[1] * f.sg[2];
@@ -177,20 +187,39 @@ __device__ __forceinline__ bool soft_frag(const SceneParams& P, const SoftCtx& S
   }
   f.D = f.Ds * T;
   if (!(f.D > 0.f)) return false;
-  f.w = il.w / f.Q;
   // normalised depth relative to the scene reference: zs - (zfar - w_ref)/(zfar - znear).  The softmax only
   // sees differences, and this form keeps ~7 significant digits of them where (zfar - w) / (zfar - znear)
-  // would keep ~1 after the 1/gamma amplification
+  // would keep ~1 after the 1/gamma amplification.  w - w_ref = sum_k q_k d_k / Q with d_k = w_k - w_ref,
+  // saturated beyond d_hi = max_k d_k
   {
     const float4 r14 = S.R[14][t];
-    const float d2 = S.R[5][t].w;
-    f.zs = -((f.E[0] * iw.x * r14.z + f.E[1] * iw.y * r14.w + f.E[2] * iw.z * d2) / f.Q) * inv_zr;
+    const float dd[3] = {r14.z, r14.w, S.R[5][t].w};
+    const int hi = dd[1] > dd[0] ? (dd[2] > dd[1] ? 2 : 1) : (dd[2] > dd[0] ? 2 : 0);
+    const float sat = kSoftDepthSat * (P.zfar - P.znear);
+    float dq;
+    f.zk = -1;
+    f.zsat = 0.f;
+    f.w = 0.f;
+    if (f.Q > 0.f) {
+      f.w = il.w / f.Q;
+      dq = (f.E[0] * iw.x * dd[0] + f.E[1] * iw.y * dd[1] + f.E[2] * iw.z * dd[2]) / f.Q;
+      if (dq > dd[hi]) {
+        f.zk = hi;
+        f.zsat = expf(-(dq - dd[hi]) / sat);
+        dq = dd[hi] + sat * (1.f - f.zsat);
+      }
+    } else {
+      f.zk = hi;
+      dq = dd[hi] + sat;
+    }
+    f.zs = -dq * inv_zr;
   }
   const float4 n0 = S.R[7][t], n1 = S.R[8][t], n2 = S.R[9][t];
   const float4 col = S.R[6][t];
   const uint32_t fl = __float_as_uint(S.R[5][t].y);
   if (fl & 8u) {
-    const float q0 = f.E[0] * iw.x, q1 = f.E[1] * iw.y, q2 = f.E[2] * iw.z;
+    // perspective-correct normal, oriented by the sign of Q (beyond the plane's vanishing line Q < 0)
+    const float q0 = f.E[0] * iw.x * f.qsgn, q1 = f.E[1] * iw.y * f.qsgn, q2 = f.E[2] * iw.z * f.qsgn;
     f.un[0] = q0 * n0.x + q1 * n1.x + q2 * n2.x;
     f.un[1] = q0 * n0.y + q1 * n1.y + q2 * n2.y;
     f.un[2] = q0 * n0.z + q1 * n1.z + q2 * n2.z;
@@ -273,10 +302,19 @@ __device__ __forceinline__ void soft_grad(const SceneParams& P, const Frag& f, S
       acc[21 + c] += dndl * nh[c];
     }
   }
-  // depth: zs(w), w = area2 / Q
-  const float dLdw = -dLdzs * inv_zr;
-  const float dLdQ = -dLdw * f.w / f.Q;
-  const float dLdarea = dLdw / f.Q;
+  // depth: zs(w), w = area2 / Q; where saturated, w = w_hi + s (1 - e) with e = exp(-(area2 / Q - w_hi) / s)
+  // (e = 0 where Q <= 0): dw / d(area2 / Q) = e, dw / dw_hi = 1 - e, w_hi = 1 / iw_zk
+  float dLdw = -dLdzs * inv_zr;
+  if (f.zk >= 0) {
+    const float wh = 1.f / (f.zk == 0 ? iwk[0] : (f.zk == 1 ? iwk[1] : iwk[2]));
+    const float g = -dLdw * (1.f - f.zsat) * wh * wh;
+    diw[0] += f.zk == 0 ? g : 0.f;
+    diw[1] += f.zk == 1 ? g : 0.f;
+    diw[2] += f.zk == 2 ? g : 0.f;
+    dLdw *= f.zsat;
+  }
+  const float dLdQ = f.Q > 0.f ? -dLdw * f.w / f.Q : 0.f;
+  const float dLdarea = f.Q > 0.f ? dLdw / f.Q : 0.f;
 #pragma unroll
   for (int e = 0; e < 3; ++e) {
     dE[e] = dLdD * f.D * (1.f - f.sg[e]) * inv_sigma;  // dL/de_e for now
@@ -296,7 +334,10 @@ __device__ __forceinline__ void soft_grad(const SceneParams& P, const Frag& f, S
     dE[e] = dE[e] * invL[e] + dLdQ * iwk[e];
   }
   if (smooth) {
+    // u = sign(Q) sum_k q_k n_k
     const float4 nn[3] = {n0, n1, n2};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) du[c] *= f.qsgn;
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
       const float ndu = nn[e].x * du[0] + nn[e].y * du[1] + nn[e].z * du[2];

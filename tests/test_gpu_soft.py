@@ -2,9 +2,10 @@
 kernel against the dense float64 PyTorch reference gradient and against FP64
 central finite differences (Richardson-extrapolated, step 1e-4).
 
-Tolerances: forward |GPU - FP64| <= 2e-4 per channel; gradients, as a
-norm-wise relative error over all checked parameters, <= 1e-4 (measured
-values are printed with -s)."""
+Tolerances: forward |GPU - FP64| <= 2e-4 per channel; gradients against
+finite differences, as a norm-wise relative error over all checked
+parameters, <= 1e-5 (the value is in the assertion message and printed with
+-s); against the dense float64 model, the float32 floor stated below."""
 import numpy as np
 import pytest
 import torch
@@ -110,13 +111,22 @@ def test_soft_gradients_match_dense_torch_reference(cuda):
     assert max(errs.values()) <= 2e-3, errs
 
 
-def test_soft_cartpole_fd_check(cuda):
+@pytest.mark.parametrize("sigma", [None, 0.5], ids=["edge10to90_0.5px", "sigma_0.5px"])
+def test_soft_cartpole_fd_check(cuda, sigma):
     """Differentiable CartPole: 8 scenes at 64x64, loss = MSE against targets
     rendered at states perturbed by N(0, 0.05); gradients w.r.t. per-instance
     position, HPR and colour and the light direction, against FP64 central
-    finite differences with step 1e-4 (Richardson-extrapolated)."""
+    finite differences with step 1e-4 (Richardson-extrapolated), as a
+    norm-wise relative error over all 147 parameters.  Two readings of
+    "sigmoid edge width 0.5 px": the default sigma = 0.5 / (2 ln 9) px (the
+    10-90 % rise of the edge sigmoid spans 0.5 px), bar 1e-5; and
+    sigma = 0.5 px, bar 1e-4.  The float64 model itself is smooth at both (its
+    exact gradient and these finite differences agree to 5e-9 and 2e-8); what
+    is left is the float32 floor of the kernels' geometry, which weighs more
+    at sigma = 0.5 px, where the loss gradient is 5x smaller for a similar
+    absolute error (measured 9.1e-6 and 4.7e-5)."""
     n = 8
-    r = soft_cartpole(n)
+    r = soft_cartpole(n, **({} if sigma is None else {"soft_sigma": sigma}))
     st = workloads.cartpole_states(n, seed=35, device=cuda)
     noisy = st + torch.randn(st.shape, generator=torch.Generator().manual_seed(36)).to(cuda) * 0.05
     r._step(noisy)
@@ -139,8 +149,10 @@ def test_soft_cartpole_fd_check(cuda):
         got.append(float(g_light[i]))
         want.append(fd_light(sc, me, no, tgt, i))
     err = rel_err(got, want)
-    print(f"soft CartPole FD check: {len(got)} parameters, relative error {err:.3e}")
-    assert err <= 1e-4
+    msg = f"soft CartPole FD check (sigma {sc['sigma']:.4f} px): {len(got)} parameters, relative error {err:.3e}"
+    print(msg)
+    assert len(got) == 147, msg
+    assert err <= (1e-5 if sigma is None else 1e-4), msg
 
 
 def test_soft_step_and_optimisation(cuda):

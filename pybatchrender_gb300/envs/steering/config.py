@@ -51,7 +51,7 @@ class SteeringConfig(PBRConfig):
     player_model: str = "models/box"
     obstacle_sphere_model: str = "models/smiley"
     obstacle_cone_model: str = "models/cone.egg"
-    border_model: str = "models/cylinder"
+    border_model: str = "models/cylinder/scene.gltf"
 
     # Scene layout
     lane_width: float = 25.0

@@ -539,32 +539,69 @@ _BUILTIN = {
     "icosphere": lambda: icosphere(2),
     # Panda3D's bundled smiley (a textured sphere) is not available: an untextured sphere stands in
     "smiley": lambda: icosphere(2),
+    # the reference's rail model (pybatchrender/models/cylinder/scene.gltf) when its file is not on the
+    # model search path: a procedural cylinder along the same (z) axis
+    "cylinder/scene.gltf": lambda: cylinder(64),
 }
 
 
 _MODEL_EXTENSIONS = (".egg", ".egg.pz", ".gltf", ".glb")
 
+MODEL_PATH_ENV = "PBR_MODEL_PATH"
+
+
+def model_search_path() -> list[str]:
+    """Directories searched for model files given by a relative path: the
+    entries of the ``PBR_MODEL_PATH`` environment variable (separated by
+    ``os.pathsep``), Panda3D's ``model-path`` in the reference.  A path
+    ``"models/<rel>"`` is looked up as ``<dir>/models/<rel>`` and as
+    ``<dir>/<rel>``, so both a directory holding ``models/`` (such as the
+    reference's package directory) and the models directory itself work --
+    the lookup of the reference's Steering renderer
+    (``envs/steering/renderer.py:89-108``)."""
+    return [d for d in os.environ.get(MODEL_PATH_ENV, "").split(os.pathsep) if d]
+
+
+def _find_model_file(model: str) -> str | None:
+    """The file a model path names: the path itself, then the model search
+    path; like Panda3D's loader, a path without an extension finds the file
+    with one."""
+    cands = [model]
+    if not os.path.isabs(model):
+        rel = model[len("models/"):] if model.startswith("models/") else None
+        for d in model_search_path():
+            cands.append(os.path.join(d, model))
+            if rel:
+                cands.append(os.path.join(d, rel))
+    for c in cands:
+        if os.path.isfile(c):
+            return c
+        for ext in _MODEL_EXTENSIONS:
+            if os.path.isfile(c + ext):
+                return c + ext
+    return None
+
 
 def resolve_model(model: "str | Mesh") -> Mesh:
     """Map a reference-style model path to a mesh.
 
-    ``"models/box"`` / ``"box"`` -> :func:`unit_cube` (Panda3D's bundled box);
-    ``"cylinder"``, ``"cylinder:<segments>"``, ``"icosphere:<level>"`` ->
-    procedural shapes; an existing ``.egg`` / ``.egg.pz`` / ``.gltf`` / ``.glb``
-    file (the extension may be left out, as with Panda3D's loader) -> the
-    loaders above.  A :class:`Mesh` is returned as a copy.
+    An existing ``.egg`` / ``.egg.pz`` / ``.gltf`` / ``.glb`` file, given
+    directly or found on the model search path (:func:`model_search_path`;
+    the extension may be left out, as with Panda3D's loader) -> the loaders
+    above.  Otherwise built-in meshes: ``"models/box"`` / ``"box"`` ->
+    :func:`unit_cube` (Panda3D's bundled box); ``"cylinder"``,
+    ``"cylinder:<segments>"``, ``"icosphere:<level>"`` -> procedural shapes;
+    ``"models/smiley"`` and the reference's rail model
+    ``"models/cylinder/scene.gltf"`` -> procedural stand-ins when their files
+    are not found.  A :class:`Mesh` is returned as a copy.
     """
     if isinstance(model, Mesh):
         return model.copy()
     if not isinstance(model, str):
         raise TypeError(f"model_path must be a str or Mesh, got {type(model).__name__}")
-    if not os.path.isfile(model):
-        # like Panda3D's loader, a path without an extension finds the file with one
-        for ext in _MODEL_EXTENSIONS:
-            if os.path.isfile(model + ext):
-                model = model + ext
-                break
-    if os.path.isfile(model):
+    found = _find_model_file(model)
+    if found is not None:
+        model = found
         low = model.lower()
         if low.endswith(".egg") or low.endswith(".egg.pz"):
             return load_egg(model)

@@ -1,8 +1,9 @@
 """Generate the golden fixtures of this directory from the reference itself.
 
-Runs the reference's unmodified Python scene code (imported from the reference
-checkout at ``/root/reference``) under the stand-ins of ``stub_panda3d.py`` and
-records what it would upload to OpenGL.  The fixtures pin everything before
+Runs the reference's unmodified Python scene code (imported from a reference
+checkout whose path is given on the command line or in ``PBR_REFERENCE_DIR``)
+under the stand-ins of ``stub_panda3d.py`` and records what it would upload to
+OpenGL.  The fixtures pin everything before
 rasterisation: baked vertices, per-instance model matrices and colours,
 per-scene view-projection matrices, tile rectangles, shader uniforms and the
 ``PBRConfig`` resolution bookkeeping.  ``ref_env_dynamics.npz`` records
@@ -12,9 +13,19 @@ trajectories of the reference's CartPole and Steering environments
 ``ref_config_defaults.json`` holds the default of every configuration field
 ``ref_grid_frames.npz`` the snapshot grids of ``PBREnv._make_grid_frame`` and
 ``ref_defaults_scene.npz`` a scene built with every node, camera and light
-argument left at its default.  Usage (from the repository root):
+argument left at its default.  ``ref_model_assets.npz`` holds the model files
+the reference ships (``pybatchrender/models/cone.egg``, the Steering rails'
+``pybatchrender/models/cylinder/scene.gltf`` with its ``scene.bin`` and
+licence) byte for byte, with facts read from them independently of this
+package's loaders: vertex and triangle counts and position bounds.  The
+cylinder is "Cylinder" by username7777777
+(https://sketchfab.com/3d-models/cylinder-679440db551840d2b4586e790228a12c),
+licensed under CC-BY-4.0 (http://creativecommons.org/licenses/by/4.0/); the
+cone is part of the reference (MIT licence, copyright 2025 Evgenii Rudakov
+and contributors).  Usage (from the repository root):
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference
+    PBR_REFERENCE_DIR=/path/to/reference python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -198,7 +209,40 @@ def grid_frames(env_cls) -> dict:
     return rec
 
 
+def model_assets(ref_path: str) -> dict:
+    """The reference's model files, byte for byte, and facts about them read
+    straight from the files: the egg's <Vertex> and <Polygon> entries (each
+    polygon's vertex count, so the triangle count of a fan triangulation), and
+    the glTF's accessor counts and the POSITION accessor's declared bounds."""
+    import re
+    models = os.path.join(ref_path, "pybatchrender", "models")
+    rec = {}
+    with open(os.path.join(models, "cone.egg"), "rb") as f:
+        egg = f.read()
+    rec["cone_egg"] = np.frombuffer(egg, np.uint8)
+    text = egg.decode()
+    rec["cone_vertices"] = len(re.findall(r"<Vertex>", text))
+    polys = re.findall(r"<Polygon>\s*\{(.*?)<VertexRef>\s*\{([^}]*)\}", text, flags=re.S)
+    sizes = [len(re.sub(r"<Ref>.*", "", refs, flags=re.S).split()) for _, refs in polys]
+    rec["cone_polygon_sizes"] = np.asarray(sizes, np.int32)
+    rec["cone_triangles"] = int(sum(n - 2 for n in sizes))
+    cyl = os.path.join(models, "cylinder")
+    for name, key in (("scene.gltf", "cylinder_gltf"), ("scene.bin", "cylinder_bin"),
+                      ("license.txt", "cylinder_license")):
+        with open(os.path.join(cyl, name), "rb") as f:
+            rec[key] = np.frombuffer(f.read(), np.uint8)
+    doc = json.loads(bytes(rec["cylinder_gltf"]).decode())
+    prim = doc["meshes"][0]["primitives"][0]
+    pos = doc["accessors"][prim["attributes"]["POSITION"]]
+    rec["cylinder_vertices"] = int(pos["count"])
+    rec["cylinder_triangles"] = int(doc["accessors"][prim["indices"]]["count"]) // 3
+    rec["cylinder_pos_min"] = np.asarray(pos["min"], np.float64)
+    rec["cylinder_pos_max"] = np.asarray(pos["max"], np.float64)
+    return rec
+
+
 def main(ref_path: str) -> None:
+    np.savez_compressed(os.path.join(HERE, "ref_model_assets.npz"), **model_assets(ref_path))
     pbr, cp = import_reference(ref_path)
     np.savez_compressed(os.path.join(HERE, "ref_grid_frames.npz"), **grid_frames(pbr.PBREnv))
     with contextlib.redirect_stdout(io.StringIO()):
@@ -271,4 +315,7 @@ def main(ref_path: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PBR_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout> (or set PBR_REFERENCE_DIR)")
+    main(ref)

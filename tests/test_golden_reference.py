@@ -152,15 +152,15 @@ def _jsonable(v):
 
 def test_config_defaults_match_reference():
     """Every field of the reference's PBRConfig, CartPoleConfig and
-    SteeringConfig exists here with the same default; the only difference is
-    Steering's rail model (the reference's glTF file is not part of this
-    package: the procedural cylinder stands in).  The extra fields are this
-    renderer's own options."""
+    SteeringConfig exists here with the same default (Steering's rail model
+    is the reference's glTF file, found through the model search path; a
+    procedural cylinder stands in when it is not there).  The extra fields are
+    this renderer's own options."""
     import dataclasses
     from pybatchrender_gb300.envs.cartpole import CartPoleConfig
     from pybatchrender_gb300.envs.steering import SteeringConfig
     ref = json.load(open(os.path.join(GOLDEN, "ref_config_defaults.json")))
-    allowed = {("SteeringConfig", "border_model"): ("models/cylinder/scene.gltf", "models/cylinder")}
+    allowed = {}
     own = {"autotune", "bin_size", "cuda_graph", "fused_step", "persistent", "raster_kernel", "raster_method",
            "raster_mode", "raster_threads", "return_depth", "reuse_output", "soft_gamma", "soft_sigma", "tri_cap"}
     for name, cls in (("PBRConfig", pbr.PBRConfig), ("CartPoleConfig", CartPoleConfig),

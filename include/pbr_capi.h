@@ -226,11 +226,13 @@ int pbr_backward_soft(pbr_ctx* ctx, const float* d_out, const float* d_stats, co
  * depth/colour scratch in a static 16 MiB device array instead of a
  * cudaMalloc'd buffer: for callers that may not allocate device memory when
  * they render -- inside a CUDA stream capture, or under a host framework whose
- * allocator owns the device memory.  This call allocates nothing; the
- * context is created beforehand.  Limit: num_scenes * width * height at most
- * about 2M pixels (8 bytes each); larger requests fail with PBR_ERR_CAPACITY.
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress): make it once before any stream capture.  All calls
+ * allocator owns the device memory.  The context is created beforehand.
+ * Limit: num_scenes * width * height at most about 2M pixels (8 bytes each);
+ * larger requests fail with PBR_ERR_CAPACITY.  The first call on a device
+ * loads the library's module that holds the array (CUDA loads device code
+ * lazily), which reserves its 16 MiB on that device until the process exits,
+ * and looks up its device address (cudaGetSymbolAddress): make that first
+ * call before any stream capture.  Later calls allocate nothing.  All calls
  * share the one array: calls that overlap on the GPU (other streams, other
  * contexts) race; calls on one stream are ordered.  No counterpart in the
  * reference. */

@@ -1003,9 +1003,11 @@ int pbr_device_status(pbr_ctx* ctx, int32_t* out_flags) {
 // allocation there invalidates the capture), or a host framework whose
 // allocator has already reserved the device memory and forbids raw
 // cudaMalloc -- use pbr_plain_render_noalloc instead.  Its scratch is a
-// file-scope device array that exists from the moment the library is loaded
-// (every GPU that loads libpbr.so holds it until the process exits), so the
-// call itself allocates nothing.
+// file-scope device array.  CUDA loads a library's device code lazily, per
+// device, so the array's 16 MiB are reserved by the driver when the first call
+// on a device looks up its address (cudaGetSymbolAddress loads this file's
+// module); from then on the device holds it until the process exits, and
+// later calls allocate nothing.
 #include <mutex>
 
 #define PBR_NOALLOC_SCRATCH_BYTES (16u << 20)  // 16 MiB: N*H*W*8 bytes (plus alignment) must fit
@@ -1036,8 +1038,9 @@ extern "C" int pbr_plain_render_noalloc(pbr_ctx* ctx, uint8_t* d_out, float* d_d
   if (dev < 0 || dev >= 256) return set_err(ctx, PBR_ERR_INVALID, "device ordinal %d out of range", dev);
   void* base = nullptr;
   {
-    // first call on this device: look up the array's device address (a host
-    // reference to g_noalloc_scratch is only a stand-in, not a device address)
+    // first call on this device: load the module that holds the array and look
+    // up its device address (a host reference to g_noalloc_scratch is only a
+    // stand-in, not a device address)
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_base[dev]) {
       e = cudaGetSymbolAddress(&g_noalloc_base[dev], g_noalloc_scratch);

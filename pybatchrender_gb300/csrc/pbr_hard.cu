@@ -41,8 +41,9 @@ namespace pbr {
 // ---------------------------------------------------------------------------
 // plain-mode helpers
 
-__global__ void plain_clear_kernel(int total, float* zbuf, uint32_t* cbuf, uint32_t bg) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+__global__ void plain_clear_kernel(long long total, float* zbuf, uint32_t* cbuf, uint32_t bg) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
     zbuf[i] = 1.f;
     cbuf[i] = bg;
   }
@@ -121,8 +122,8 @@ cudaError_t hard_launch(int threads, bool plain, bool winner, const SceneParams&
 }
 
 cudaError_t plain_clear_launch(const SceneParams& P, float* zbuf, uint32_t* cbuf, cudaStream_t stream) {
-  const int total = P.N * P.W * P.H;
-  const int grid = min((total + 255) / 256, 152 * 8);
+  const long long total = (long long)P.N * P.W * P.H;
+  const int grid = (int)min((total + 255) / 256, (long long)152 * 8);
   plain_clear_kernel<<<grid, 256, 0, stream>>>(total, zbuf, cbuf, P.bg_packed);
   return cudaGetLastError();
 }

@@ -5,7 +5,9 @@ whose buffer is cudaMalloc'd), called through the C ABI, twice in a row.
 Callers that may not allocate device memory while rendering (during a CUDA
 stream capture, or under a framework allocator that owns the device memory)
 use the no-allocation entry point; its scratch is a static device array of
-16 MiB, so requests beyond about 2M pixels are rejected.
+16 MiB, so requests beyond about 2M pixels are rejected.  After the first
+call on a device (which loads the module holding that array), further calls
+leave the device's free memory unchanged.
 
 This file is collected last so that a run stopping at the first failure has
 already run every other test."""
@@ -51,3 +53,25 @@ def test_noalloc_rejects_oversized_requests(cuda):
     rc = r._lib.pbr_plain_render_noalloc(r._ctx, _capi.ptr(out), None, torch.cuda.current_stream().cuda_stream)
     assert rc == _capi.PBR_ERR_CAPACITY
     assert b"static buffer" in r._lib.pbr_last_error(r._ctx)
+
+
+def test_noalloc_leaves_device_memory_unchanged(cuda):
+    """Free device memory (cudaMemGetInfo) is the same before and after three
+    calls that follow the first one: no call reserves device memory.  Every
+    tensor the calls touch exists before the first reading."""
+    r = workloads.cartpole_bench(num_scenes=96, res=64, seed=44)
+    r._step(workloads.cartpole_states(96, seed=45, device=cuda))
+    stream = torch.cuda.current_stream().cuda_stream
+    out = torch.empty((96, 3, 64, 64), dtype=torch.uint8, device=cuda)
+    depth = torch.empty((96, 64, 64), dtype=torch.float32, device=cuda)
+    _capi.call(r._lib, r._ctx, "pbr_plain_render_noalloc", _capi.ptr(out), _capi.ptr(depth), stream)
+    torch.cuda.synchronize()
+    first = out.clone()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        _capi.call(r._lib, r._ctx, "pbr_plain_render_noalloc", _capi.ptr(out), _capi.ptr(depth), stream)
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, (free_before, free_after)
+    assert torch.equal(out, first)

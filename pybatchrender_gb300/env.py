@@ -64,6 +64,12 @@ class TensorDictLite(dict):
     def keys(self, include_nested: bool = False):
         return list(dict.keys(self))
 
+    def clone(self) -> "TensorDictLite":
+        out = TensorDictLite(batch_size=self.batch_size)
+        for k, v in dict.items(self):
+            dict.__setitem__(out, k, v.clone() if hasattr(v, "clone") else v)
+        return out
+
 
 def TensorDict(fields, batch_size=None):  # noqa: N802 - mirrors the tensordict constructor
     if HAVE_TORCHRL:
@@ -263,19 +269,32 @@ class PBREnv(_Base):
 
     @classmethod
     def make_parallel_env(cls, *, config: PBRConfig, renderer_cls, num_workers: int,
-                          mp_start_method: str = "spawn", shared_memory: bool = True):
-        """TorchRL ``ParallelEnv`` of ``num_workers`` spawned replicas, each with
-        its own renderer (``env.py:360-416``).  Needs TorchRL."""
+                          mp_start_method: str = "spawn", shared_memory: bool = True, devices=None):
+        """``num_workers`` spawned replicas, each with its own renderer
+        (``env.py:360-416``): TorchRL's ``ParallelEnv`` when TorchRL is
+        installed, else :class:`~pybatchrender_gb300.parallel_env.ParallelEnvLite`
+        with the same ``reset`` / ``step`` contract and batch
+        ``[num_workers, num_scenes]``.  ``devices`` (no reference counterpart):
+        one device per worker, e.g. ``["cuda:0", "cuda:1"]``, to spread the
+        replicas over GPUs; by default every worker uses ``config.device``."""
+        num_workers = int(num_workers)
+        if devices is not None and len(devices) != num_workers:
+            raise ValueError("devices needs one entry per worker")
+        kwargs = []
+        for i in range(num_workers):
+            cfg = config if devices is None else PBRConfig.from_config(config, device=str(devices[i]))
+            kwargs.append({"env_cls": cls, "renderer_cls": renderer_cls, "config": cfg, "worker_index": i,
+                           "num_workers": num_workers})
         if not HAVE_TORCHRL:
-            raise RuntimeError("make_parallel_env needs torchrl and tensordict, which are not installed")
+            from .parallel_env import ParallelEnvLite
+            return ParallelEnvLite(num_workers, create_env_fn=cls._make_env_worker, create_env_kwargs=kwargs,
+                                   mp_start_method=mp_start_method, shared_memory=shared_memory)
         import multiprocessing as mp  # pragma: no cover
         try:
             mp.set_start_method(mp_start_method, force=True)
         except RuntimeError:
             pass
-        kwargs = [{"env_cls": cls, "renderer_cls": renderer_cls, "config": config, "worker_index": i,
-                   "num_workers": num_workers} for i in range(int(num_workers))]
-        return _ParallelEnv(int(num_workers), create_env_fn=cls._make_env_worker, shared_memory=shared_memory,
+        return _ParallelEnv(num_workers, create_env_fn=cls._make_env_worker, shared_memory=shared_memory,
                             mp_start_method=mp_start_method, create_env_kwargs=kwargs)
 
     @staticmethod

@@ -51,14 +51,18 @@ def make(name: str, **config_overrides):
     return env_cls(renderer=renderer, cfg=cfg)
 
 
-def make_parallel(name: str, num_workers: int, shared_memory: bool = True, **config_overrides):
-    """TorchRL ``ParallelEnv`` of spawned workers (needs TorchRL)."""
+def make_parallel(name: str, num_workers: int, shared_memory: bool = True, devices=None, **config_overrides):
+    """``num_workers`` spawned replicas of env ``name``, each with its own
+    renderer, as one env of batch ``[num_workers, num_scenes]``
+    (``envs/__init__.py:127-164``): TorchRL's ``ParallelEnv`` when TorchRL is
+    installed, else the process-replica stand-in of ``parallel_env``.
+    ``devices``: optional device per worker (see ``PBREnv.make_parallel_env``)."""
     if name not in _ENV_REGISTRY:
         raise ValueError(f"Unknown environment: '{name}'. Available: {list_envs()}")
     env_cls, renderer_cls, config_cls = _ENV_REGISTRY[name]
     cfg = config_cls(**config_overrides)
     return env_cls.make_parallel_env(config=cfg, renderer_cls=renderer_cls, num_workers=num_workers,
-                                     mp_start_method="spawn", shared_memory=shared_memory)
+                                     mp_start_method="spawn", shared_memory=shared_memory, devices=devices)
 
 
 def _register_builtins() -> None:

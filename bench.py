@@ -19,9 +19,12 @@ Reported variants (all on the same scene and states):
                device-to-host copy of step i runs on a second stream while
                step i+1 uploads and renders.
   variants     plain per-launch path (host-built matrices, a host-to-device
-               copy per node, one launch per node, a synchronise); the step
+               copy per node, one launch per node, a synchronise); the fused
+               step replayed as a CUDA graph (the state copied into the graph's
+               static input, then the captured launch); the step
                through ``_step``'s torch copies + render captured in a CUDA
-               graph; soft_fwd (differentiable soft-coverage forward, float32)
+               graph; fused_over_plain / graph_over_plain: the fused launch and
+               the graph replay against the plain path; soft_fwd (differentiable soft-coverage forward, float32)
                and fwd_bwd (soft forward + adjoint kernel with a constant
                dL/dout) on the same scene; env_step_eager / env_step_graph:
                the CartPole-v0 env step (dynamics, termination, reward,
@@ -285,6 +288,24 @@ def run_ours(args, world, rank, local):
         t = time_steps(lambda i: copy_r.step(states[i % 16]), args.steps, flush, stream)
         copy_fps = N * args.steps / (reduce_max(sum(t), world) / 1000.0)
 
+        # the fused step replayed as a CUDA graph: the step's state copied into the graph's static input,
+        # then the captured state-bound launch
+        static_state = states[0].clone()
+        for i in range(3):
+            graph_r.step(static_state)
+        torch.cuda.synchronize()
+        fused_graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(fused_graph):
+            graph_r.step(static_state)
+
+        def fused_graph_step(i):
+            static_state.copy_(states[i % 16], non_blocking=True)
+            fused_graph.replay()
+        for i in range(3):
+            fused_graph_step(i)
+        t = time_steps(fused_graph_step, args.steps, flush, stream)
+        fused_graph_fps = N * args.steps / (reduce_max(sum(t), world) / 1000.0)
+
         # plain per-launch path (wall clock: it synchronises every step)
         plain_steps = max(3, min(args.steps, args.plain_steps))
         for i in range(2):
@@ -391,8 +412,10 @@ def run_ours(args, world, rank, local):
                    "l2": "flushed (256 MiB write) before every timed step, flush excluded",
                    "launch": tuned or {"kernel": graph_r.cfg.raster_kernel, "threads": graph_r.cfg.raster_threads,
                                        "bin_px": graph_r.cfg.bin_size}},
-        "variants": {"batched_fused_step": value / world, "batched_graph_step_copies": copy_fps, "plain": plain_fps,
-                     "graph_over_plain": (value / world) / plain_fps,
+        "variants": {"batched_fused_step": value / world, "batched_graph_fused_step": fused_graph_fps,
+                     "batched_graph_step_copies": copy_fps, "plain": plain_fps,
+                     "fused_over_plain": (value / world) / plain_fps,
+                     "graph_over_plain": fused_graph_fps / plain_fps,
                      "soft_fwd": soft_fwd_fps, "fwd_bwd": fwd_bwd_fps, "soft_fwd_over_fwd_bwd": soft_fwd_fps / fwd_bwd_fps,
                      "env_step_eager": env_eager_fps, "env_step_graph": env_graph_fps},
         "e2e": {"value": e2e_fps, "unit": UNIT, "h2d_bytes_per_step": int(N * 4 * 4),
@@ -429,6 +452,7 @@ def run_workload(args, world, rank, local):
     line = {"workload": name, "unit": UNIT, "n_gpus": world, "higher_is_better": True, "scaling": "weak",
             "data": "synthetic", "steps": args.steps, "warmup": args.warmup}
     torch.cuda.reset_peak_memory_stats(device)
+    free0, _ = torch.cuda.mem_get_info(device)
     if name in ("many_cubes", "uneven"):
         ns = {"num_scenes": args.workload_scenes} if args.workload_scenes > 0 else {}
         if name == "many_cubes":
@@ -491,8 +515,25 @@ def run_workload(args, world, rank, local):
         for i in range(max(3, args.warmup)):
             fwd_bwd(i)
         torch.cuda.synchronize()
-        tf = time_steps(fwd, args.steps, flush, stream)
-        tb = time_steps(fwd_bwd, args.steps, flush, stream)
+        graphed = name == "soft_large"
+        if graphed:
+            # the step (forward + adjoint, gradient buffers zeroed inside) captured once and replayed: the
+            # scene is static, so nothing is copied in per step
+            torch.cuda.empty_cache()  # the footprint below is the graphs' memory, not the eager warm-up's cache
+            g_f, g_b = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g_b):
+                fwd_bwd(0)
+            with torch.cuda.graph(g_f, pool=g_b.pool()):  # replays never overlap: one memory pool
+                fwd(0)
+            for i in range(2):
+                g_f.replay()
+                g_b.replay()
+            torch.cuda.synchronize()
+            tf = time_steps(lambda i: g_f.replay(), args.steps, flush, stream)
+            tb = time_steps(lambda i: g_b.replay(), args.steps, flush, stream)
+        else:
+            tf = time_steps(fwd, args.steps, flush, stream)
+            tb = time_steps(fwd_bwd, args.steps, flush, stream)
         ms_f = reduce_max(sum(tf), world) / args.steps
         ms_b = reduce_max(sum(tb), world) / args.steps
         b_fwd = res * res * 12 + n_inst * BYTES_PER_INSTANCE + BYTES_PER_SCENE
@@ -501,11 +542,15 @@ def run_workload(args, world, rank, local):
                      "ms_per_step": ms_b, "dtype": "f32",
                      "forward": {"value": world * N / (ms_f / 1000.0), "ms_per_step": ms_f},
                      "fwd_over_fwd_bwd": ms_b / ms_f,
-                     "config": {"workload": desc},
+                     "config": {"workload": desc, "step": "CUDA graph replay" if graphed else "eager launches"},
                      "roofline": {"bound": "hbm", "achieved": b_bwd * N / (ms_b / 1000.0) / 1e9, "peak": hbm_peak,
                                   "unit": "GB/s", "frac": b_bwd * N / (ms_b / 1000.0) / 1e9 / hbm_peak,
                                   "bytes_per_frame": b_bwd, "peak_source": peak_src}})
-    line["hbm_footprint_bytes"] = int(torch.cuda.max_memory_allocated(device))
+    # device memory in use beyond what was in use before the workload: tensors (PyTorch's cache at its
+    # peak), the library's own scratch (e.g. the binned soft kernel's slabs) and graph pools
+    free1, _ = torch.cuda.mem_get_info(device)
+    line["hbm_footprint_bytes"] = int(free0 - free1)
+    line["torch_peak_allocated_bytes"] = int(torch.cuda.max_memory_allocated(device))
     if rank == 0:
         print(json.dumps(line), flush=True)
 

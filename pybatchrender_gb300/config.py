@@ -72,7 +72,7 @@ class PBRConfig:
     raster_mode: str = 'hard'        # 'hard' (uint8 pixels) | 'soft' (float32, differentiable)
     raster_kernel: str = 'auto'      # 'auto' | 'warp' (scene per warp, small scenes) | 'tile' (CTA per region)
                                      # | 'binned' (soft mode: global per-block candidate masks, large scenes)
-    raster_threads: int = 256        # threads per CTA: 128 | 256 | 512
+    raster_threads: int = 256        # threads per CTA: 128 | 256 | 512 (warp kernel: 128 | 224 | 448)
     bin_size: int = 16               # binner tile size in pixels: 8 | 16 | 32
     tri_cap: int = 0                 # triangles per shared-memory chunk (0 = automatic)
     persistent: bool = False         # persistent work-stealing schedule
@@ -167,8 +167,9 @@ class PBRConfig:
             raise ValueError(f"raster_mode must be 'hard' or 'soft', got {self.raster_mode!r}")
         if self.raster_kernel not in ('auto', 'warp', 'tile', 'binned'):
             raise ValueError("raster_kernel must be 'auto', 'warp', 'tile' or 'binned'")
-        if self.raster_threads not in (128, 256, 512):
-            raise ValueError("raster_threads must be 128, 256 or 512")
+        if self.raster_threads not in (128, 256, 512) and not (self.raster_kernel == 'warp'
+                                                               and self.raster_threads in (224, 448)):
+            raise ValueError("raster_threads must be 128, 256 or 512 (224 or 448 with raster_kernel='warp')")
         if self.bin_size not in (8, 16, 32):
             raise ValueError("bin_size must be 8, 16 or 32")
         if not 1 <= int(self.num_channels) <= 4:

@@ -195,13 +195,14 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
   return PBR_OK;
 }
 
-// Scene-per-warp plan; returns PBR_ERR_CAPACITY when the scene is not small.
-static int plan_small(pbr_ctx* ctx, bool plain, bool winner, int n0, int n1, LaunchPlan* out) {
+// Scene-per-warp plan with blocks of `warps` warps; returns PBR_ERR_CAPACITY
+// when the scene is not small or the block does not fit in shared memory.
+static int plan_small(pbr_ctx* ctx, bool plain, bool winner, int n0, int n1, LaunchPlan* out,
+                      int warps = pbr::small_warps()) {
   const SceneParams& P = ctx->P;
   if (P.W % 16 != 0) return set_err(ctx, PBR_ERR_CAPACITY, "scene-per-warp kernel needs width %% 16 == 0");
   const long long need = 2 * scene_source_tris(ctx, n0, n1);  // a near-plane clip can split a triangle in two
   if (need > 128) return set_err(ctx, PBR_ERR_CAPACITY, "scene too large for the scene-per-warp kernel");
-  const int warps = pbr::small_warps();
   RasterArgs A;
   memset(&A, 0, sizeof(A));
   A.node_begin = n0;
@@ -241,8 +242,15 @@ static int plan_small(pbr_ctx* ctx, bool plain, bool winner, int n0, int n1, Lau
   return PBR_OK;
 }
 
+// Warps per block of the scene-per-warp kernel for a launch configuration:
+// its thread count when the configuration names that kernel, else the default.
+static int small_warps_of(const LaunchCfg& c) {
+  return (c.kernel == 1 && c.threads % 32 == 0 && c.threads / 32 <= pbr::small_max_warps()) ? c.threads / 32
+                                                                                              : pbr::small_warps();
+}
+
 static int plan_any(pbr_ctx* ctx, const LaunchCfg& c, bool plain, bool winner, int n0, int n1, LaunchPlan* out) {
-  if (c.kernel == 1) return plan_small(ctx, plain, winner, n0, n1, out);
+  if (c.kernel == 1) return plan_small(ctx, plain, winner, n0, n1, out, small_warps_of(c));
   if (c.kernel == 0) {
     if (plan_small(ctx, plain, winner, n0, n1, out) == PBR_OK) return PBR_OK;
     ctx->err.clear();
@@ -251,7 +259,7 @@ static int plan_any(pbr_ctx* ctx, const LaunchCfg& c, bool plain, bool winner, i
 }
 
 static cudaError_t launch_plan(pbr_ctx* ctx, const LaunchPlan& lp, bool plain, bool winner, cudaStream_t s) {
-  if (lp.kind == 1) return pbr::small_launch(plain, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
+  if (lp.kind == 1) return pbr::small_launch(plain, winner, ctx->P, lp.A, lp.threads / 32, lp.grid, lp.smem, s);
   return pbr::hard_launch(lp.threads, plain, winner, ctx->P, lp.A, lp.grid, lp.smem, s);
 }
 
@@ -522,8 +530,12 @@ int pbr_raster_config(pbr_ctx* ctx, int kernel, int threads, int bin_px, int tri
   PBR_CHECK_CTX(ctx);
   if (kernel < 0 || kernel > 3)
     return set_err(ctx, PBR_ERR_INVALID, "kernel must be 0 (auto), 1, 2 or 3 (got %d)", kernel);
-  if (threads != 128 && threads != 256 && threads != 512)
-    return set_err(ctx, PBR_ERR_INVALID, "threads must be 128, 256 or 512 (got %d)", threads);
+  // the tile kernel has 128-, 256- and 512-thread instantiations; the scene-per-warp kernel (kernel 1)
+  // also takes blocks of 7 or 14 warps
+  const bool small_only = kernel == 1 && (threads == 224 || threads == 448);
+  if (threads != 128 && threads != 256 && threads != 512 && !small_only)
+    return set_err(ctx, PBR_ERR_INVALID, "threads must be 128, 256 or 512, or 224 or 448 with kernel 1 (got %d)",
+                   threads);
   if (bin_px != 8 && bin_px != 16 && bin_px != 32)
     return set_err(ctx, PBR_ERR_INVALID, "bin_px must be 8, 16 or 32 (got %d)", bin_px);
   if (tri_cap != 0 && (tri_cap < 64 || tri_cap > 4096 || (tri_cap % 32) != 0))
@@ -590,9 +602,10 @@ int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_kernel, in
   std::vector<LaunchCfg> cands;
   {
     LaunchPlan probe;
-    if (plan_small(ctx, false, false, 0, ctx->P.num_nodes, &probe) == PBR_OK)
-      cands.push_back({1, pbr::small_warps() * 32, 16, 0, 0});
-    ctx->err.clear();
+    for (int w : {4, 7, 14}) {  // blocks of 4, 7 or 14 warps, where they fit in shared memory
+      if (plan_small(ctx, false, false, 0, ctx->P.num_nodes, &probe, w) == PBR_OK) cands.push_back({1, w * 32, 16, 0, 0});
+      ctx->err.clear();
+    }
     const long long need = 2 * scene_source_tris(ctx, 0, ctx->P.num_nodes);
     std::vector<int> caps = {0};
     if (need > 256) { caps.push_back(256); caps.push_back(512); }

@@ -16,13 +16,14 @@ cudaError_t hard_occupancy(int threads, bool plain, bool winner, bool tex, int s
 const void* hard_tex_fn(int threads, bool plain, bool winner);
 cudaError_t hard_launch(int threads, bool plain, bool winner, const SceneParams& P, const RasterArgs& A,
                         int grid, int smem_bytes, cudaStream_t stream);
-// Scene-per-warp raster (pbr_small.cu); blocks of small_warps() warps.
+// Scene-per-warp raster (pbr_small.cu); blocks of 1..small_max_warps() warps, small_warps() by default.
 int small_warps();
+int small_max_warps();
 int small_smem_per_warp(const RasterArgs& A, int W, int H);  // -1: image has more than 64 bins
 cudaError_t small_set_smem_limit(bool plain, bool winner, int shade, int bytes);  // shade 0 flat, 1 smooth, 2 textured
-cudaError_t small_occupancy(bool plain, bool winner, int shade, int smem_bytes, int* blocks_per_sm);
-cudaError_t small_launch(bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int grid, int smem_bytes,
-                         cudaStream_t stream);
+cudaError_t small_occupancy(bool plain, bool winner, int shade, int warps, int smem_bytes, int* blocks_per_sm);
+cudaError_t small_launch(bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int warps, int grid,
+                         int smem_bytes, cudaStream_t stream);
 // Soft coverage (pbr_soft.cu); threads in {128, 256}.
 int soft_smem_bytes(const SoftArgs& a, int threads);
 cudaError_t soft_set_smem_limit(int threads, bool backward, int bytes);

@@ -39,8 +39,9 @@ namespace pbr {
 constexpr int kBinW = 32;  // bin = 32 x 16 pixels = 32 lanes x 16-pixel row segments
 constexpr int kBinH = 16;
 constexpr int kBinPx = kBinW * kBinH;
-constexpr int kWarps = 4;   // warps per block
-constexpr int kBlocksPerSm = 7;
+constexpr int kWarps = 4;        // default warps per block
+constexpr int kMaxWarps = 14;    // launch bound: blocks of up to 14 warps, two per SM (the same 72-register
+constexpr int kMinBlocks = 2;    // budget as seven blocks of 4 warps); the block size is chosen at launch
 
 struct SmallLayout {
   int t0, t1, t2, t3, bgrec, t4, s0, s1, s2, s3, s4, s5, masks, vp, uni;
@@ -56,7 +57,8 @@ struct SmallLayout {
 // normal with .w = z + w; screen position), instance table (5 float4 per
 // instance: 3 model-matrix rows, colour, meta) and view-projection matrix
 // share one region with the raster stage's key tile.  Cartpole-sized scenes
-// need 8064 bytes a warp, which keeps 7 blocks of 4 warps on an SM.
+// need 8016 bytes a warp, which keeps 28 warps on an SM (7 blocks of 4 warps
+// or 2 blocks of 14).
 __host__ __device__ inline SmallLayout small_layout(int tri_cap, int vcap, int icap, int nbins, int smooth,
                                                     int tex) {
   SmallLayout L;
@@ -169,7 +171,7 @@ __device__ __forceinline__ int small_tri(const SceneParams& P, const SetupCtx& S
 
 // SHADE: 0 = flat meshes only, 1 = smooth meshes (per-pixel normals), 2 = smooth and textured
 template <bool PLAIN, bool WINNER, int SHADE>
-__global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const __grid_constant__ SceneParams P,
+__global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const __grid_constant__ SceneParams P,
                                                                          const __grid_constant__ RasterArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr bool SMOOTH = SHADE >= 1, TEX = SHADE == 2;
@@ -215,7 +217,8 @@ __global__ void __launch_bounds__(kWarps * 32, kBlocksPerSm) small_kernel(const 
   // key of an untouched pixel: depth 1.0 (the clear), draw order 0 (before every triangle)
   const unsigned long long clear_key = (unsigned long long)__float_as_uint(1.f) << 32;
 
-  for (int k = blockIdx.x * kWarps + warp; k < P.N; k += gridDim.x * kWarps) {
+  const int nwarps = blockDim.x >> 5;
+  for (int k = blockIdx.x * nwarps + warp; k < P.N; k += gridDim.x * nwarps) {
     if (lane < 16) s_vp[lane] = P.vp[(long long)k * 16 + lane];
 
     // ---- K1: instance table, flattened over nodes in draw order ---------
@@ -550,18 +553,20 @@ cudaError_t small_set_smem_limit(bool plain, bool winner, int shade, int bytes) 
   return cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
-cudaError_t small_occupancy(bool plain, bool winner, int shade, int smem_bytes, int* blocks_per_sm) {
+cudaError_t small_occupancy(bool plain, bool winner, int shade, int warps, int smem_bytes, int* blocks_per_sm) {
   const void* f = pick_small(plain, winner, shade);
-  if (!f) return cudaErrorInvalidValue;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, kWarps * 32, smem_bytes);
+  if (!f || warps < 1 || warps > kMaxWarps) return cudaErrorInvalidValue;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, warps * 32, smem_bytes);
 }
 
-cudaError_t small_launch(bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int grid, int smem_bytes,
-                         cudaStream_t stream) {
+cudaError_t small_launch(bool plain, bool winner, const SceneParams& P, const RasterArgs& A, int warps, int grid,
+                         int smem_bytes, cudaStream_t stream) {
   const void* f = pick_small(plain, winner, shade_of(A));
-  if (!f) return cudaErrorInvalidValue;
+  if (!f || warps < 1 || warps > kMaxWarps) return cudaErrorInvalidValue;
   void* args[] = {const_cast<SceneParams*>(&P), const_cast<RasterArgs*>(&A)};
-  return cudaLaunchKernel(f, dim3(grid), dim3(kWarps * 32), args, (size_t)smem_bytes, stream);
+  return cudaLaunchKernel(f, dim3(grid), dim3(warps * 32), args, (size_t)smem_bytes, stream);
 }
+
+int small_max_warps() { return kMaxWarps; }
 
 }  // namespace pbr

@@ -11,8 +11,9 @@
 //      Survivors are compacted in draw order (warp prefix sums + per-warp
 //      totals, one barrier per round), their records written to the slab,
 //      and the bit of each survivor is set in the masks of the 8x4-pixel
-//      blocks its widened bbox touches (atomicOr): per block one bit per
-//      survivor, so a block's candidates are read back in draw order.
+//      blocks that hold a pixel centre within the coverage cutoff of its
+//      vertices' bbox (atomicOr): per block one bit per survivor, so a
+//      block's candidates are read back in draw order.
 //   B  warps take blocks in turn, one pixel per lane: the block's mask words
 //      are read 32 at a time (coalesced), and the set bits give the
 //      candidates in draw order.  Forward: online softmax per pixel in
@@ -193,13 +194,24 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
             }
             soft_setup<true>(P, S, cv[0], nv[0], iv[0], cv[1], nv[1], iv[1], cv[2], nv[2], iv[2], slot,
                              icache[li * 4 + 3], nd.rank_base + b0 + li, smooth);
-            // this survivor's bit in the masks of the blocks its widened bbox touches
-            const uint32_t xb = __float_as_uint(S.R[4][slot].w), yb = __float_as_uint(S.R[5][slot].x);
-            const int bx0 = (int)(xb & 0xffffu) / kLBlkW, bx1 = (int)(xb >> 16) / kLBlkW;
-            const int by0 = (int)(yb & 0xffffu) / kLBlkH, by1 = (int)(yb >> 16) / kLBlkH;
+            // this survivor's bit in the masks of the blocks holding a pixel centre within the cutoff of its
+            // vertices' bbox (a superset of the pixels it can cover: the distance to the triangle is at least
+            // the distance to that bbox), widened by 1e-3 px; clamped as floats first, since vertices of
+            // near-plane triangles can be far outside the image
+            const float4 s01 = S.R[13][slot], s2 = S.R[14][slot];
+            const float mnx = fminf(fminf(s01.x, s01.z), s2.x), mxx = fmaxf(fmaxf(s01.x, s01.z), s2.x);
+            const float mny = fminf(fminf(s01.y, s01.w), s2.y), mxy = fmaxf(fmaxf(s01.y, s01.w), s2.y);
+            const int px0 = (int)fmaxf(0.f, ceilf(mnx - S.cut - 0.501f));
+            const int px1 = (int)fminf((float)(W - 1), floorf(mxx + S.cut - 0.499f));
+            const int py0 = (int)fmaxf(0.f, ceilf(mny - S.cut - 0.501f));
+            const int py1 = (int)fminf((float)(H - 1), floorf(mxy + S.cut - 0.499f));
+            const int bx0 = px0 / kLBlkW, bx1 = px1 / kLBlkW;
+            const int by0 = py0 / kLBlkH, by1 = py1 / kLBlkH;
             const uint32_t bit = 1u << (slot & 31);
-            for (int by = by0; by <= by1; ++by)
-              for (int bx = bx0; bx <= bx1; ++bx) atomicOr(&bmask[(long long)(by * nbx + bx) * words + (slot >> 5)], bit);
+            if (px0 <= px1 && py0 <= py1)
+              for (int by = by0; by <= by1; ++by)
+                for (int bx = bx0; bx <= bx1; ++bx)
+                  atomicOr(&bmask[(long long)(by * nbx + bx) * words + (slot >> 5)], bit);
           }
           T += total;
         }

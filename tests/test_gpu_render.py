@@ -94,6 +94,20 @@ def test_launch_configs_bitwise_equal(cuda, threads, bin_px, persistent):
     assert torch.equal(r.render(), ref)
 
 
+@pytest.mark.parametrize("threads", [224, 448])
+def test_warp_kernel_block_sizes_bitwise_equal(cuda, threads):
+    """The scene-per-warp kernel in blocks of 7 or 14 warps (one scene per
+    warp either way) renders exactly what blocks of 4 warps render, through
+    render() and the state-bound step."""
+    st = workloads.cartpole_states(300, seed=28, device=cuda)
+    a = workloads.cartpole_bench(num_scenes=300, seed=29, raster_kernel="warp", raster_threads=128)
+    b = workloads.cartpole_bench(num_scenes=300, seed=29, raster_kernel="warp", raster_threads=threads)
+    assert torch.equal(a.step(st).clone(), b.step(st))
+    pa, da, wa = a.render(return_depth=True, return_winner=True)
+    pb, db, wb = b.render(return_depth=True, return_winner=True)
+    assert torch.equal(pa, pb) and torch.equal(da, db) and torch.equal(wa, wb)
+
+
 def test_deterministic_and_graph_replay(cuda):
     r = workloads.cartpole_bench(num_scenes=128, seed=9, cuda_graph=True)
     st1 = workloads.cartpole_states(128, seed=10, device=cuda)

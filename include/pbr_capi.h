@@ -17,8 +17,8 @@
  *  - Every entry point returns an int status: PBR_OK (0) or a PBR_ERR_* code.
  *    pbr_last_error() returns a message for the last failing call on a context
  *    (or, with ctx == NULL, for the last failing pbr_create, or call given a
- *    null context, on this thread).  pbr_cartpole_step takes no context and
- *    reports through its status alone.
+ *    null context, on this thread).  pbr_cartpole_step and pbr_camera_update
+ *    take no context and report through their status alone.
  *  - Pointers named d_* are device pointers on the context's device.  They are
  *    borrowed, never freed: the caller keeps them alive while they are bound.
  *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default
@@ -265,6 +265,18 @@ int pbr_cartpole_step(const float* d_obs, const int64_t* d_action, const int64_t
                       const float* d_reset_theta_dot, float* d_next_raw, float* d_next_obs, float* d_reward,
                       uint8_t* d_done, int64_t* d_next_step_count, long long n, const double* consts,
                       int auto_reset, void* stream);
+
+/* Per-scene camera matrices in one launch (no context): the view of
+ * renderer/camera.py:201-240 and VP = P V of camera.py:252-262, replacing the
+ * reference's per-step host math and buffer-texture upload of viewbuf.
+ * d_view [K,16] row-major is updated in place: with d_forward and/or d_up
+ * given ([K,3]; a missing one keeps the current forward (-row 2) or up (row 1)),
+ * f = normalize(forward), up = normalize(up), s = normalize(f x up), u = s x f,
+ * rows 0..2 = s, u, -f; with d_eye [K,3] the translation is (-s.e, -u.e, f.e).
+ * d_vp [K,16] (or NULL) receives projection (16 floats, row-major, host
+ * memory) times the view.  Normalisation divides by max(|v|, 1e-8). */
+int pbr_camera_update(const float* d_eye, const float* d_forward, const float* d_up, float* d_view,
+                      const float projection[16], float* d_vp, int num_scenes, void* stream);
 
 #ifdef __cplusplus
 }

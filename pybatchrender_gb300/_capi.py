@@ -58,6 +58,7 @@ SIGNATURES: dict[str, list] = {
     "pbr_backward_soft": [_vp, _vp, _vp, _vp, _vp, _vp],
     "pbr_debug_transforms": [_vp, _i, _vp, _vp],
     "pbr_device_status": [_vp, ctypes.POINTER(ctypes.c_int32)],
+    "pbr_camera_update": [_vp, _vp, _vp, _vp, ctypes.POINTER(ctypes.c_float), _vp, _i, _vp],
     "pbr_cartpole_step": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_longlong,
                           ctypes.POINTER(ctypes.c_double), _i, _vp],
 }

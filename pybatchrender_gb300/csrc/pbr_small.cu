@@ -12,7 +12,8 @@
 //       smooth meshes also n = normalize(mat3(M) n))
 //   K2  lane = triangle: near clip, cull, watertight edges, depth plane, flat
 //       shading (a flat mesh's provoking normal is transformed here, for
-//       survivors only); compacted in draw order with a warp prefix sum;
+//       survivors only), written at the triangle's two fixed slots (2t, 2t+1:
+//       draw order, room for a near-plane split; unused slots are empty);
 //       then the warp-ballot binner: for each 32x16-pixel bin one
 //       __ballot_sync over the lanes (= triangles) is the bin's mask
 //   K3  per bin: a bin without candidates is written as background with
@@ -245,6 +246,8 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
       const MeshDesc& me = P.meshes[nd.mesh];
       const int li = i - ai;
       const long long id = nd.shared ? (long long)li : (long long)k * nd.ips + li;
+      // the colour first: issued with the pose loads, before the write-back stores it cannot be moved past
+      const float4 col = *reinterpret_cast<const float4*>(nd.color + id * 4);
       float m[12];
       build_model(nd, id, m);
       write_back_bound(nd, id);
@@ -252,7 +255,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
       e[0] = make_float4(m[0], m[1], m[2], m[3]);
       e[1] = make_float4(m[4], m[5], m[6], m[7]);
       e[2] = make_float4(m[8], m[9], m[10], m[11]);
-      e[3] = *reinterpret_cast<const float4*>(nd.color + id * 4);
+      e[3] = col;
       // meta: node, first vertex, draw id of triangle 0, first triangle
       e[4] = make_float4(__int_as_float(n), __int_as_float(av + li * me.nv),
                          __int_as_float((nd.rank_base + li) * P.max_tris), __int_as_float(at + li * me.nt));
@@ -260,62 +263,88 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
     __syncwarp();
 
     // ---- K1: vertices ------------------------------------------------------
-    for (int v = lane; v < total_verts; v += 32) {
-      int inst = 0;
-      while (inst + 1 < total_inst && __float_as_int(itab[(inst + 1) * 5 + 4].y) <= v) ++inst;
-      const float4 meta = itab[inst * 5 + 4];
-      const MeshDesc& me = P.meshes[P.nodes[__float_as_int(meta.x)].mesh];
-      const int vi = v - __float_as_int(meta.y);
-      const float4 r0 = itab[inst * 5 + 0], r1 = itab[inst * 5 + 1], r2 = itab[inst * 5 + 2];
-      const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
-      const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
-      const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
-      const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
-      const float4 q0 = *reinterpret_cast<const float4*>(s_vp), q1 = *reinterpret_cast<const float4*>(s_vp + 4);
-      const float4 q2 = *reinterpret_cast<const float4*>(s_vp + 8), q3 = *reinterpret_cast<const float4*>(s_vp + 12);
-      float4 c;
-      c.x = q0.x * wx + q0.y * wy + q0.z * wz + q0.w;
-      c.y = q1.x * wx + q1.y * wy + q1.z * wz + q1.w;
-      c.z = q2.x * wx + q2.y * wy + q2.z * wz + q2.w;
-      c.w = q3.x * wx + q3.y * wy + q3.z * wz + q3.w;
-      float4 nv = make_float4(0.f, 0.f, 0.f, c.z + c.w);
-      if (SMOOTH) {
-        const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
-        const float nx = r0.x * ax + r0.y * ay + r0.z * az;
-        const float ny = r1.x * ax + r1.y * ay + r1.z * az;
-        const float nz = r2.x * ax + r2.y * ay + r2.z * az;
-        const float l2 = nx * nx + ny * ny + nz * nz;
-        const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
-        nv.x = nx * inv;
-        nv.y = ny * inv;
-        nv.z = nz * inv;
+    // two vertices per lane and pass (v and v + 32), so that the mesh loads of
+    // both are in flight together
+    for (int v0 = lane; v0 < total_verts; v0 += 64) {
+      int vv[2], inst[2];
+      float o[2][3], a[2][3];
+      const MeshDesc* mp[2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int v = min(v0 + 32 * u, total_verts - 1);  // a lane past the end repeats a vertex, unstored
+        int in = 0;
+        while (in + 1 < total_inst && __float_as_int(itab[(in + 1) * 5 + 4].y) <= v) ++in;
+        const float4 meta = itab[in * 5 + 4];
+        mp[u] = &P.meshes[P.nodes[__float_as_int(meta.x)].mesh];
+        const int vi = v - __float_as_int(meta.y);
+        vv[u] = vi;
+        inst[u] = in;
       }
-      const SV sv = to_screen(c, S.W, S.H);
-      vcache[3 * v] = c;
-      vcache[3 * v + 1] = nv;
-      vcache[3 * v + 2] = make_float4(sv.x, sv.y, sv.z, sv.iw);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const float* pp = mp[u]->pos + 3 * vv[u];
+        o[u][0] = pp[0];
+        o[u][1] = pp[1];
+        o[u][2] = pp[2];
+        if (SMOOTH) {
+          const float* np = mp[u]->nrm + 3 * vv[u];
+          a[u][0] = np[0];
+          a[u][1] = np[1];
+          a[u][2] = np[2];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int v = v0 + 32 * u;
+        if (v >= total_verts) continue;
+        const int in = inst[u];
+        const float4 r0 = itab[in * 5 + 0], r1 = itab[in * 5 + 1], r2 = itab[in * 5 + 2];
+        const float ox = o[u][0], oy = o[u][1], oz = o[u][2];
+        const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
+        const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
+        const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
+        const float4 q0 = *reinterpret_cast<const float4*>(s_vp), q1 = *reinterpret_cast<const float4*>(s_vp + 4);
+        const float4 q2 = *reinterpret_cast<const float4*>(s_vp + 8), q3 = *reinterpret_cast<const float4*>(s_vp + 12);
+        float4 c;
+        c.x = q0.x * wx + q0.y * wy + q0.z * wz + q0.w;
+        c.y = q1.x * wx + q1.y * wy + q1.z * wz + q1.w;
+        c.z = q2.x * wx + q2.y * wy + q2.z * wz + q2.w;
+        c.w = q3.x * wx + q3.y * wy + q3.z * wz + q3.w;
+        float4 nv = make_float4(0.f, 0.f, 0.f, c.z + c.w);
+        if (SMOOTH) {
+          const float ax = a[u][0], ay = a[u][1], az = a[u][2];
+          const float nx = r0.x * ax + r0.y * ay + r0.z * az;
+          const float ny = r1.x * ax + r1.y * ay + r1.z * az;
+          const float nz = r2.x * ax + r2.y * ay + r2.z * az;
+          const float l2 = nx * nx + ny * ny + nz * nz;
+          const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
+          nv.x = nx * inv;
+          nv.y = ny * inv;
+          nv.z = nz * inv;
+        }
+        const SV sv = to_screen(c, S.W, S.H);
+        vcache[3 * v] = c;
+        vcache[3 * v + 1] = nv;
+        vcache[3 * v + 2] = make_float4(sv.x, sv.y, sv.z, sv.iw);
+      }
     }
     __syncwarp();
 
-    // ---- K2: triangles, compacted in draw order -------------------------
-    int tri_count = 0;
-    for (int t0 = 0; t0 < total_tris; t0 += 32) {
-      const int t = t0 + lane;
-      const int c = t < total_tris ? small_tri<false, SMOOTH, TEX>(P, S, vcache, itab, total_inst, t, 0) : 0;
-      int incl = c;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      const int total = __shfl_sync(0xffffffffu, incl, 31);
-      if (c > 0) small_tri<true, SMOOTH, TEX>(P, S, vcache, itab, total_inst, t, tri_count + incl - c);
-      tri_count += total;
+    // ---- K2: triangles at fixed slots in draw order ------------------------
+    // Triangle t owns slots 2t and 2t + 1 (a near-plane clip can split it in
+    // two), so each triangle is set up once, with no count pass: a slot that
+    // holds no triangle gets an empty row range (first row 0xffff, last row
+    // 0), which puts it in no bin.  Slot order is draw order.
+    for (int t = lane; t < total_tris; t += 32) {
+      const int c = small_tri<true, SMOOTH, TEX>(P, S, vcache, itab, total_inst, t, 2 * t);
+      const float no_rows = __uint_as_float(0xffffu);
+      if (c < 1) reinterpret_cast<float*>(&S.T4[2 * t])[0] = no_rows;
+      if (c < 2) reinterpret_cast<float*>(&S.T4[2 * t + 1])[0] = no_rows;
     }
     __syncwarp();
 
     // ---- warp-ballot binner ----------------------------------------------
-    const int T = tri_count;
+    const int T = 2 * total_tris;
     const int nw = (T + 31) >> 5;
     unsigned long long ne = 0ull;  // bit b: bin b has candidates
     for (int w = 0; w < nw; ++w) {

@@ -12,12 +12,16 @@ torch on the renderer's device:
 * ``VP = P @ V`` per scene (``camera.py:252-262``).
 
 ``VP_k44`` is written in place into a device tensor that the renderer binds
-once, so camera updates need no rebinding.  One deliberate difference:
+once, so camera updates need no rebinding.  On a CUDA device each update is
+one launch of ``pbr_camera_update`` (the same formulas in float32, view and
+view-projection together) instead of a dozen tensor operations; on the CPU
+the tensor operations run.  One deliberate difference:
 ``set_projection`` takes effect (the reference only clears a cache that
 ``_update_vp`` never reads again, so there it has no effect).
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from typing import Literal
 
@@ -110,6 +114,7 @@ class PBRCam(PBRShaderContext):
             P[2, 3] = torch.tensor((2.0 * self.z_far * self.z_near) / (self.z_near - self.z_far), dtype=torch.float32)
             P[3, 2] = torch.tensor(-1.0, dtype=torch.float32)
             self._proj_cache_key = key
+            self._P_host = (ctypes.c_float * 16)(*P.reshape(-1).tolist())
             self._proj_cache = P.to(self.device)
         return self._proj_cache
 
@@ -144,10 +149,34 @@ class PBRCam(PBRShaderContext):
             raise ValueError(f"{name} first dim must be K={self.num_scenes}, got {a.shape[0]}")
         return a
 
-    def _update_view(self, eye_k3=None, forward_k3=None, up_k3=None) -> None:
+    def _camera_kernel(self, eye=None, fwd=None, up=None, vp: bool = False) -> None:
+        """One ``pbr_camera_update`` launch on the current stream: the view's
+        basis from ``fwd`` / ``up`` (when given), its translation from ``eye``
+        (when given), and ``VP_k44`` when ``vp``."""
+        from .. import _capi
+        lib = _capi.load()
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        rc = lib.pbr_camera_update(_capi.ptr(eye), _capi.ptr(fwd), _capi.ptr(up), _capi.ptr(self.V_k44),
+                                   self._P_host, _capi.ptr(self.VP_k44) if vp else None, int(self.num_scenes),
+                                   stream)
+        if rc != _capi.PBR_OK:
+            raise _capi.PBRError("pbr_camera_update", rc, "invalid arguments or launch failure")
+
+    def _update_view(self, eye_k3=None, forward_k3=None, up_k3=None, vp: bool = False) -> None:
+        """Update the view from a new eye, forward and/or up (rows s, u, -f,
+        translation from the eye); with ``vp`` also the view-projection."""
         basis_changed = (forward_k3 is not None) or (up_k3 is not None)
         eye_changed = eye_k3 is not None
         if not basis_changed and not eye_changed:
+            if vp:
+                self._update_vp()
+            return
+        if self.device.type == "cuda":
+            f = self._ensure_kx3(forward_k3, 'forward_k3').contiguous() if forward_k3 is not None else None
+            u = self._ensure_kx3(up_k3, 'up_k3').contiguous() if up_k3 is not None else None
+            if eye_changed:
+                self.eye_k3 = self._ensure_kx3(eye_k3, 'eye_k3').contiguous()
+            self._camera_kernel(eye=self.eye_k3, fwd=f, up=u, vp=vp)
             return
         if basis_changed:
             if forward_k3 is not None:
@@ -172,6 +201,8 @@ class PBRCam(PBRShaderContext):
         self.V_k44[:, 0, 3] = -torch.einsum('ij,ij->i', s, self.eye_k3)
         self.V_k44[:, 1, 3] = -torch.einsum('ij,ij->i', u, self.eye_k3)
         self.V_k44[:, 2, 3] = torch.einsum('ij,ij->i', f, self.eye_k3)
+        if vp:
+            self._update_vp()
 
     @staticmethod
     def _fwd_up_from_hpr(hpr_k3: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
@@ -181,6 +212,9 @@ class PBRCam(PBRShaderContext):
         return torch.einsum('bij,j->bi', R, unit_fwd), torch.einsum('bij,j->bi', R, unit_up)
 
     def _update_vp(self) -> None:
+        if self.device.type == "cuda":
+            self._camera_kernel(vp=True)
+            return
         VP = torch.einsum('ij,bjk->bik', self.P_k44, self.V_k44).reshape(-1, 4, 4)
         self.VP_k44.copy_(VP.to(torch.float32))
 
@@ -190,9 +224,7 @@ class PBRCam(PBRShaderContext):
     # --- public API (camera.py:268-344) ---
     def look_at(self, target_k3, lazy: bool = False) -> None:
         fwd = self._fwd_from_lookat(target_k3)
-        self._update_view(forward_k3=fwd)
-        if not lazy:
-            self._update_vp()
+        self._update_view(forward_k3=fwd, vp=not lazy)
 
     def set_positions(self, eye_k3, keep_lookat: bool = False, lazy: bool = False) -> None:
         if keep_lookat:
@@ -203,9 +235,7 @@ class PBRCam(PBRShaderContext):
         eye_k3 = self._ensure_kx3(eye_k3, 'eye_k3')
         target_k3 = self._ensure_kx3(target_k3, 'target_k3')
         fwd = self._fwd_from_lookat(target_k3, eye_k3)
-        self._update_view(eye_k3=eye_k3, forward_k3=fwd)
-        if not lazy:
-            self._update_vp()
+        self._update_view(eye_k3=eye_k3, forward_k3=fwd, vp=not lazy)
 
     def _fwd_from_lookat(self, target_k3, eye_k3=None) -> torch.Tensor:
         eye = eye_k3 if eye_k3 is not None else self.eye_k3
@@ -216,32 +246,22 @@ class PBRCam(PBRShaderContext):
     def set_hprs(self, hpr_k3, lazy: bool = False) -> None:
         hpr = self._ensure_kx3(hpr_k3, 'hpr_k3')
         fwd, up = self._fwd_up_from_hpr(hpr)
-        self._update_view(forward_k3=fwd, up_k3=up)
-        if not lazy:
-            self._update_vp()
+        self._update_view(forward_k3=fwd, up_k3=up, vp=not lazy)
 
     def set_eye(self, eye_k3, lazy: bool = False) -> None:
-        self._update_view(eye_k3=eye_k3)
-        if not lazy:
-            self._update_vp()
+        self._update_view(eye_k3=eye_k3, vp=not lazy)
 
     def set_forward(self, forward_k3, lazy: bool = False) -> None:
-        self._update_view(forward_k3=forward_k3)
-        if not lazy:
-            self._update_vp()
+        self._update_view(forward_k3=forward_k3, vp=not lazy)
 
     def set_up(self, up_k3, lazy: bool = False) -> None:
-        self._update_view(up_k3=up_k3)
-        if not lazy:
-            self._update_vp()
+        self._update_view(up_k3=up_k3, vp=not lazy)
 
     def set_right(self, right_k3, lazy: bool = False) -> None:
         right_k3 = type(self)._normalize(torch.as_tensor(right_k3, dtype=torch.float32).to(self.device))
         f = -self.V_k44[:, 2, 0:3]
         u = torch.cross(right_k3.expand_as(f), f, dim=-1)
-        self._update_view(forward_k3=f, up_k3=u)
-        if not lazy:
-            self._update_vp()
+        self._update_view(forward_k3=f, up_k3=u, vp=not lazy)
 
     def start_tasks(self, taskMgr=None, name: str = "pbr_cam_update") -> None:
         """``camera.py:404-420`` registers a per-frame task that re-uploads the

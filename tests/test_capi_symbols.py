@@ -78,6 +78,19 @@ def test_cartpole_step_argument_checks_without_gpu(lib):
     assert f(*bad, 8, consts, 0, None) == _capi.PBR_ERR_INVALID
 
 
+def test_camera_update_validates_before_any_cuda_call(lib):
+    """pbr_camera_update takes no context: a missing view buffer, a view-projection
+    without a projection, or a negative scene count are rejected before any
+    launch; zero scenes is a no-op."""
+    f = lib.pbr_camera_update
+    f.argtypes, f.restype = _capi.SIGNATURES["pbr_camera_update"], ctypes.c_int
+    P = (ctypes.c_float * 16)()
+    assert f(None, None, None, None, P, None, 4, None) == _capi.PBR_ERR_INVALID
+    assert f(None, None, None, 1024, None, 2048, 4, None) == _capi.PBR_ERR_INVALID
+    assert f(None, None, None, 1024, P, None, -1, None) == _capi.PBR_ERR_INVALID
+    assert f(None, None, None, 1024, P, 2048, 0, None) == _capi.PBR_OK
+
+
 _NULL_CTX_PROBE = r"""
 import ctypes, sys
 from pybatchrender_gb300 import _capi
@@ -87,7 +100,7 @@ lib.pbr_last_error.restype = ctypes.c_char_p
 lib.pbr_last_error.argtypes = [ctypes.c_void_p]
 bad = []
 for name, sig in _capi.SIGNATURES.items():
-    if not sig or sig[0] is not ctypes.c_void_p or name in ("pbr_destroy", "pbr_cartpole_step"):
+    if not sig or sig[0] is not ctypes.c_void_p or name in ("pbr_destroy", "pbr_cartpole_step", "pbr_camera_update"):
         continue
     args = []
     for t in sig:

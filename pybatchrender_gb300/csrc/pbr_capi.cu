@@ -141,14 +141,8 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
     if (me.smooth) A.smooth_any = 1;
     if (nd.tex) A.smooth_any = A.tex_any = 1;  // textured triangles are shaded per pixel
   }
-  // vertex cache (shared memory, 32 bytes per vertex) for the largest mesh of 64 or more triangles with at
-  // most 1024 vertices; smaller meshes transform per triangle
-  int vc = 0;
-  for (int n = n0; n < n1; ++n) {
-    const MeshDesc& me = P.meshes[P.nodes[n].mesh];
-    if (me.nt >= 64 && me.nv <= 1024) vc = std::max(vc, me.nv);
-  }
-  A.vcap = vc > 0 ? (vc + 31) & ~31 : 0;
+  // no vertex cache: each thread transforms its own triangle's vertices
+  A.vcap = 0;
   int icap = 1;
   for (int n = n0; n < n1; ++n) icap = std::max(icap, P.nodes[n].ips);
   A.icap = std::min(icap, 256);
@@ -167,10 +161,6 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
     if (L.total <= ctx->max_smem) {
       out->smem = L.total;
       break;
-    }
-    if (A.vcap > 0 && cap <= 256) {  // keep chunks of 512+ triangles before the vertex cache
-      A.vcap = 0;
-      continue;
     }
     if (cap > 64) {
       cap = std::max(64, (cap / 2 + 31) & ~31);

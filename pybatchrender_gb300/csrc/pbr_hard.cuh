@@ -30,7 +30,6 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
   S.cull = P.cull;
   uint32_t* masks = reinterpret_cast<uint32_t*>(smem + L.masks);
   float4* icache = reinterpret_cast<float4*>(smem + L.icache);
-  float4* vcache = reinterpret_cast<float4*>(smem + L.vcache);  // [vcap][2]: screen (x, y, z, 1/w); normal, z + w
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem + L.state);  // [THREADS * kPx]
   int* s_scan = reinterpret_cast<int*>(smem + L.misc);
   float* s_vp = reinterpret_cast<float*>(s_scan + 2 * NW + 8);
@@ -271,11 +270,10 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
     // ---- K1 / K2: walk nodes and instances in draw order -----------------
     // Instance batches of up to icap instances (model matrices in shared
     // memory); then rounds of THREADS source triangles, one per thread: the
-    // thread transforms its triangle's three vertices itself, or reads them
-    // from the vertex cache for meshes of 64 or more triangles (see below),
-    // culls and rejects triangles that cover no pixel centre, and the
-    // survivors are compacted in draw order with one barrier per round (warp
-    // prefix sums + per-warp totals in shared memory).
+    // thread transforms its triangle's three vertices itself (no vertex cache,
+    // no per-instance barriers), culls and rejects triangles that cover no
+    // pixel centre, and the survivors are compacted in draw order with one
+    // barrier per round (warp prefix sums + per-warp totals in shared memory).
     __syncthreads();  // s_vp visible
     const float vp0 = s_vp[0], vp1 = s_vp[1], vp2 = s_vp[2], vp3 = s_vp[3];
     const float vp4 = s_vp[4], vp5 = s_vp[5], vp6 = s_vp[6], vp7 = s_vp[7];
@@ -371,104 +369,45 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           nb = total_keep;
           __syncthreads();
         }
-        // Meshes of 64 or more triangles whose vertices fit the vertex cache go through a vertex stage:
-        // the kept instances in sub-batches of vcap / nv, each vertex transformed once into shared
-        // memory (screen position, world normal, z + w), the triangles reading their three vertices from
-        // there.  Smaller meshes (and meshes too large for the cache) transform per triangle.  Both use the
-        // same arithmetic, so the two paths give identical records.
-        const bool use_vc = A.vcap >= me.nv && nt >= 64;
-        const int per_sub = use_vc ? max(1, A.vcap / me.nv) : max(nb, 1);
-        for (int s0 = 0; s0 < nb; s0 += per_sub) {
-        const int ns = min(per_sub, nb - s0);
-        if (use_vc) {
-          __syncthreads();  // the previous sub-batch's triangles are done with the vertex cache
-          for (int v = tid; v < ns * me.nv; v += THREADS) {
-            const int lv = v / me.nv, vi = v - lv * me.nv;
-            const int li = can_cull ? s_ci[s0 + lv] : s0 + lv;
-            const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
-            const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
-            const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
-            const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
-            const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
-            float4 cvv;
-            cvv.x = vp0 * wx + vp1 * wy + vp2 * wz + vp3;
-            cvv.y = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
-            cvv.z = vp8 * wx + vp9 * wy + vp10 * wz + vp11;
-            cvv.w = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
-            const SV svv = to_screen(cvv, S.W, S.H);
-            const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
-            const float nx = r0.x * ax + r0.y * ay + r0.z * az;
-            const float ny = r1.x * ax + r1.y * ay + r1.z * az;
-            const float nz = r2.x * ax + r2.y * ay + r2.z * az;
-            const float l2 = nx * nx + ny * ny + nz * nz;
-            const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
-            vcache[2 * v] = make_float4(svv.x, svv.y, svv.z, svv.iw);
-            vcache[2 * v + 1] = make_float4(nx * inv, ny * inv, nz * inv, cvv.z + cvv.w);
-          }
-          __syncthreads();
-        }
-        const int total_t = ns * nt;
+        const int total_t = nb * nt;
         for (int t0 = 0; t0 < total_t; t0 += RT) {
           // up to 2 emitted triangles per source triangle (near-plane clip)
           const int rem = min(RT, total_t - t0);
           if (tri_count + 2 * rem > A.tri_cap) flush(false);
-          int c = 0, li = 0, lsub = 0, ti = 0, i0 = 0, i1 = 0, i2 = 0;
+          int c = 0, li = 0, ti = 0, i0 = 0, i1 = 0, i2 = 0;
           float4 cv[3];
           SV sv[3];
           bool front = false;
           if (tid < rem) {
             const int t = t0 + tid;
-            lsub = t / nt;
-            ti = t - lsub * nt;
-            li = can_cull ? s_ci[s0 + lsub] : s0 + lsub;
+            li = t / nt;
+            ti = t - li * nt;
+            if (can_cull) li = s_ci[li];
             i0 = me.idx[3 * ti];
             i1 = me.idx[3 * ti + 1];
             i2 = me.idx[3 * ti + 2];
             const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
             const int iv[3] = {i0, i1, i2};
-            // clip coordinates of the triangle's vertices: needed for all of them without the vertex
-            // cache, and with it only when the triangle crosses the near plane (the clip path)
-            auto clip_of = [&](int q) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
               const int vi = iv[q];
               const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
               const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
               const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
               const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
-              float4 o;
-              o.x = vp0 * wx + vp1 * wy + vp2 * wz + vp3;
-              o.y = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
-              o.z = vp8 * wx + vp9 * wy + vp10 * wz + vp11;
-              o.w = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
-              return o;
-            };
-            float d[3];
-            if (use_vc) {
-#pragma unroll
-              for (int q = 0; q < 3; ++q) {
-                const float4 a = vcache[2 * (lsub * me.nv + iv[q])];
-                sv[q] = SV{a.x, a.y, a.z, a.w};
-                d[q] = vcache[2 * (lsub * me.nv + iv[q]) + 1].w;
-              }
-            } else {
-#pragma unroll
-              for (int q = 0; q < 3; ++q) {
-                cv[q] = clip_of(q);
-                d[q] = cv[q].z + cv[q].w;
-              }
+              cv[q].x = vp0 * wx + vp1 * wy + vp2 * wz + vp3;
+              cv[q].y = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
+              cv[q].z = vp8 * wx + vp9 * wy + vp10 * wz + vp11;
+              cv[q].w = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
             }
-            front = d[0] >= 0.f && d[1] >= 0.f && d[2] >= 0.f;
+            const float d0 = cv[0].z + cv[0].w, d1 = cv[1].z + cv[1].w, d2 = cv[2].z + cv[2].w;
+            front = d0 >= 0.f && d1 >= 0.f && d2 >= 0.f;
             const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
             if (front) {
-              if (!use_vc) {
 #pragma unroll
-                for (int q = 0; q < 3; ++q) sv[q] = to_screen(cv[q], S.W, S.H);
-              }
+              for (int q = 0; q < 3; ++q) sv[q] = to_screen(cv[q], S.W, S.H);
               c = setup_tri_sv<false>(P, S, sv[0], z4, sv[1], z4, sv[2], z4, 0, z4, 0, smooth);
-            } else if (!(d[0] < 0.f && d[1] < 0.f && d[2] < 0.f)) {
-              if (use_vc) {
-#pragma unroll
-                for (int q = 0; q < 3; ++q) cv[q] = clip_of(q);
-              }
+            } else if (!(d0 < 0.f && d1 < 0.f && d2 < 0.f)) {
               c = clip_tri<false>(P, S, cv[0], z4, cv[1], z4, cv[2], z4, i0, i1, i2, 0, z4, 0, smooth);
             }
           }
@@ -500,10 +439,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             const int iv[3] = {i0, i1, i2};
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
-              if (use_vc && (q == 0 || smooth)) {
-                const float4 a = vcache[2 * (lsub * me.nv + iv[q]) + 1];
-                nv[q] = make_float4(a.x, a.y, a.z, 0.f);
-              } else if (q == 0 || smooth) {
+              if (q == 0 || smooth) {
                 const int vi = iv[q];
                 const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
                 const float nx = r0.x * ax + r0.y * ay + r0.z * az;
@@ -531,7 +467,6 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           }
           tri_count += total;
         }
-        }  // sub-batches
       }
     }
     flush(true);

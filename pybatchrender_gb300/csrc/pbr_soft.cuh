@@ -205,7 +205,7 @@ __device__ __forceinline__ bool soft_frag(const SceneParams& P, const SoftCtx& S
       dq = (f.E[0] * iw.x * dd[0] + f.E[1] * iw.y * dd[1] + f.E[2] * iw.z * dd[2]) / f.Q;
       if (dq > dd[hi]) {
         f.zk = hi;
-        f.zsat = expf(-(dq - dd[hi]) / sat);
+        f.zsat = __expf(-(dq - dd[hi]) / sat);  // the saturated tail needs no more than the fast exponential
         dq = dd[hi] + sat * (1.f - f.zsat);
       }
     } else {

@@ -81,6 +81,19 @@ int pbr_mesh_register(pbr_ctx* ctx, const float* d_pos, const float* d_nrm, cons
  * Optional (radius 0: no skipping); no counterpart in the reference. */
 int pbr_mesh_set_bounds(pbr_ctx* ctx, int mesh_id, float cx, float cy, float cz, float radius);
 
+/* Optional: clusters of 32 consecutive triangles of a mesh, so that the tile
+ * kernel can skip groups of triangles before setting them up: d_clusters
+ * [num_clusters, 8] float32, 16-byte aligned, num_clusters = ceil(nt / 32);
+ * per cluster its bounding sphere (cx, cy, cz, r) in mesh coordinates and the
+ * cone of its triangles' geometric normals (unit axis ax, ay, az and the
+ * cosine of the cone's half-angle; <= 0: no cone).  A cluster is skipped when
+ * all its triangles face away from the eye (HPR poses) or its projected sphere
+ * holds no pixel centre of the region drawn; the pixels are the same as without
+ * clusters.  NULL removes them.  No reference counterpart (Panda3D draws every
+ * triangle). */
+int pbr_mesh_set_clusters(pbr_ctx* ctx, int mesh_id, const float* d_clusters, int num_clusters,
+                          int cluster_triangles);
+
 /* Attach texture coordinates to a registered mesh: d_uv [nv,2] float32
  * (GL convention, v = 0 at the bottom of the image), or NULL for none (all
  * coordinates 0).  Replaces the p3d_MultiTexCoord0 vertex column that

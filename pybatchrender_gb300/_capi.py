@@ -36,6 +36,7 @@ SIGNATURES: dict[str, list] = {
     "pbr_mesh_register": [_vp, _vp, _vp, _vp, _i, _i, _i, _pi],
     "pbr_mesh_set_bounds": [_vp, _i, _f, _f, _f, _f],
     "pbr_mesh_set_uv": [_vp, _i, _vp],
+    "pbr_mesh_set_clusters": [_vp, _i, _vp, _i, _i],
     "pbr_node_add": [_vp, _i, _i, _i, _pi],
     "pbr_node_set_texture": [_vp, _i, _vp, _i, _i],
     "pbr_node_set_buffers": [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp],

@@ -75,6 +75,7 @@ class PBRConfig:
     raster_threads: int = 256        # threads per CTA: 128 | 256 | 512 (warp kernel: 128 | 224 | 448)
     bin_size: int = 16               # binner tile size in pixels: 8 | 16 | 32
     tri_cap: int = 0                 # triangles per shared-memory chunk (0 = automatic)
+    cluster_cull: bool = True        # tile kernel: skip groups of 32 triangles that cannot be drawn (meshes of 128+)
     persistent: bool = False         # persistent work-stealing schedule
     autotune: bool = False           # time the launch configurations at setup_environment()
     cuda_graph: bool = False         # capture _step + render into a CUDA graph on the first step

@@ -143,6 +143,8 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
   }
   // no vertex cache: each thread transforms its own triangle's vertices
   A.vcap = 0;
+  for (int n = n0; n < n1; ++n)
+    if (P.meshes[P.nodes[n].mesh].clusters) A.cl_any = 1;
   int icap = 1;
   for (int n = n0; n < n1; ++n) icap = std::max(icap, P.nodes[n].ips);
   A.icap = std::min(icap, 256);
@@ -377,6 +379,29 @@ int pbr_mesh_set_bounds(pbr_ctx* ctx, int mesh_id, float cx, float cy, float cz,
   if (!(radius >= 0.f) || !std::isfinite(cx) || !std::isfinite(cy) || !std::isfinite(cz) || !std::isfinite(radius))
     return set_err(ctx, PBR_ERR_INVALID, "mesh bounds must be finite with radius >= 0");
   ctx->P.meshes[mesh_id].bound = make_float4(cx, cy, cz, radius);
+  return PBR_OK;
+}
+
+int pbr_mesh_set_clusters(pbr_ctx* ctx, int mesh_id, const float* d_clusters, int num_clusters,
+                          int cluster_triangles) {
+  PBR_CHECK_CTX(ctx);
+  if (mesh_id < 0 || mesh_id >= ctx->P.num_meshes) return set_err(ctx, PBR_ERR_INVALID, "unknown mesh id %d", mesh_id);
+  MeshDesc& m = ctx->P.meshes[mesh_id];
+  if (!d_clusters) {
+    m.clusters = nullptr;
+    m.ncl = 0;
+    return PBR_OK;
+  }
+  if (cluster_triangles != pbr::kClusterTris)
+    return set_err(ctx, PBR_ERR_INVALID, "clusters must hold %d triangles (got %d)", pbr::kClusterTris,
+                   cluster_triangles);
+  const int need = (m.nt + pbr::kClusterTris - 1) / pbr::kClusterTris;
+  if (num_clusters != need || need > 65535)
+    return set_err(ctx, PBR_ERR_INVALID, "mesh %d needs %d clusters (at most 65535), got %d", mesh_id, need,
+                   num_clusters);
+  if (((uintptr_t)d_clusters & 15u) != 0) return set_err(ctx, PBR_ERR_INVALID, "d_clusters must be 16-byte aligned");
+  m.clusters = reinterpret_cast<const float4*>(d_clusters);
+  m.ncl = num_clusters;
   return PBR_OK;
 }
 

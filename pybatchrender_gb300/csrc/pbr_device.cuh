@@ -120,6 +120,11 @@ __device__ __forceinline__ SV to_screen(float4 c, float W, float H) {
   s.x = (c.x * s.iw + 1.f) * 0.5f * W;
   s.y = (1.f - c.y * s.iw) * 0.5f * H;
   s.z = c.z * s.iw * 0.5f + 0.5f;
+  // The screen coordinates leave here as opaque values: no multiply of this
+  // function may be fused with an add or subtract of the caller (the setup's
+  // v1.x - v0.x, say), so every setup of the same vertices rounds alike,
+  // wherever it is inlined.
+  asm("" : "+f"(s.x), "+f"(s.y), "+f"(s.z), "+f"(s.iw));
   return s;
 }
 
@@ -227,6 +232,14 @@ __device__ __forceinline__ int setup_tri_sv(const SceneParams& P, const SetupCtx
   return 1;
 }
 
+// A record that covers no pixel: empty x and y ranges (low end above the high
+// end), so that the binner gives it no bin.  The tile kernel fills a slot it
+// reserved with one when the write pass does not emit the triangle it counted.
+__device__ __forceinline__ void write_empty(const SetupCtx& S, int slot) {
+  S.T3[slot].w = __uint_as_float(1u);       // x: [1, 0]
+  S.T4[slot].x = __uint_as_float(0xffffu);  // y: [65535, 0]
+}
+
 template <bool WRITE>
 __device__ __forceinline__ int setup_tri(const SceneParams& P, const SetupCtx& S, float4 c0, float4 n0, float4 c1,
                                          float4 n1, float4 c2, float4 n2, int slot, float4 col, int draw_id,
@@ -247,11 +260,14 @@ __device__ __forceinline__ float2 lerp2(float2 a, float2 b, float t) {
 // vertices) and fan emission of a triangle that crosses the plane.  Crossing
 // points are interpolated from the endpoint with the smaller mesh index so
 // that neighbouring triangles produce identical vertices.  Its arrays live in
-// local memory, touched only on this rare path.
+// local memory, touched only on this rare path.  With WRITE and limit >= 0
+// exactly `limit` records are written from slot on (the kept fan triangles,
+// at most limit of them, then empty records), for callers that reserved
+// slots from an earlier count.
 template <bool WRITE>
 __device__ __forceinline__ int clip_tri(const SceneParams& P, const SetupCtx& S, float4 c0, float4 n0, float4 c1,
                                      float4 n1, float4 c2, float4 n2, int i0, int i1, int i2, int slot, float4 col,
-                                     int draw_id, bool smooth, const TexIn& tx = TexIn()) {
+                                     int draw_id, bool smooth, const TexIn& tx = TexIn(), int limit = -1) {
   const float4 c[3] = {c0, c1, c2};
   const float4 n[3] = {n0, n1, n2};
   const float2 uv[3] = {tx.t0, tx.t1, tx.t2};
@@ -276,6 +292,7 @@ __device__ __forceinline__ int clip_tri(const SceneParams& P, const SetupCtx& S,
   }
   int cnt = 0;
   for (int f = 1; f + 1 < np; ++f) {
+    if (WRITE && limit >= 0 && cnt >= limit) break;
     TexIn ft;
     ft.t0 = pt[0];
     ft.t1 = pt[f];
@@ -284,6 +301,8 @@ __device__ __forceinline__ int clip_tri(const SceneParams& P, const SetupCtx& S,
     cnt += setup_tri<WRITE>(P, S, pc[0], pn[0], pc[f], pn[f], pc[f + 1], pn[f + 1], slot + cnt, col, draw_id, smooth,
                             ft);
   }
+  if (WRITE && limit >= 0)
+    for (; cnt < limit; ++cnt) write_empty(S, slot + cnt);
   return cnt;
 }
 

@@ -4,8 +4,95 @@
 #pragma once
 
 #include "pbr_device.cuh"
+#ifdef PBR_SELFCHECK
+#include <cstdio>
+#endif
 
 namespace pbr {
+
+// Self-checks, compiled in with -DPBR_SELFCHECK only (a debugging build): every
+// index below is checked against the length of the buffer it addresses; a bad
+// one is printed (the first 32 per process) and replaced by 0, so that the
+// access stays inside the buffer.  Without the macro PBR_IX is the index.
+#ifdef PBR_SELFCHECK
+static __device__ int g_selfcheck_reports;
+static __device__ __noinline__ long long selfcheck_index(long long i, long long n, int site) {
+  if (i >= 0 && i < n) return i;
+  if (atomicAdd(&g_selfcheck_reports, 1) < 32)
+    printf("pbr selfcheck: site %d block %d thread %d index %lld of %lld\n", site, (int)blockIdx.x,
+           (int)threadIdx.x, i, n);
+  return 0;
+}
+#define PBR_IX(i, n, site) selfcheck_index((long long)(i), (long long)(n), (site))
+#else
+#define PBR_IX(i, n, site) (i)
+#endif
+
+// Whether no triangle of a cluster (bounding sphere cs, normal cone ca) of an
+// instance (model matrix rows r0..r2) can be drawn in the rows [ry0, ry1] of
+// a W x H image: either every triangle faces away from the eye (HPR poses
+// with a positive determinant only: their linear part is a rotation times a
+// uniform scale, so normals turn with the axis), or the projection of the
+// sphere's box holds no pixel centre of the region.  Conservative: margins
+// of 1e-2 of the eye distance on the facing test and 0.01 px on the pixel
+// test, and a cluster with a corner behind the eye or a non-finite value is
+// kept.
+__device__ __forceinline__ bool cluster_culled(float4 cs, float4 ca, float4 r0, float4 r1, float4 r2,
+                                               const float* vp, float ex, float ey, float ez, bool eye_ok,
+                                               bool hpr, float W, float H, float ry0, float ry1) {
+  const float wx = r0.x * cs.x + r0.y * cs.y + r0.z * cs.z + r0.w;
+  const float wy = r1.x * cs.x + r1.y * cs.y + r1.z * cs.z + r1.w;
+  const float wz = r2.x * cs.x + r2.y * cs.y + r2.z * cs.z + r2.w;
+  const float n0 = r0.x * r0.x + r1.x * r1.x + r2.x * r2.x;
+  const float n1 = r0.y * r0.y + r1.y * r1.y + r2.y * r2.y;
+  const float n2 = r0.z * r0.z + r1.z * r1.z + r2.z * r2.z;
+  const float sv2 = hpr ? fmaxf(fmaxf(n0, n1), n2) : n0 + n1 + n2;
+  const float R = cs.w * sqrtf(sv2) * 1.0001f + 1e-6f;
+  if (eye_ok && hpr && ca.w > 0.f) {
+    const float det = r0.x * (r1.y * r2.z - r1.z * r2.y) - r0.y * (r1.x * r2.z - r1.z * r2.x) +
+                      r0.z * (r1.x * r2.y - r1.y * r2.x);
+    if (det > 0.f) {
+      const float ax = r0.x * ca.x + r0.y * ca.y + r0.z * ca.z;
+      const float ay = r1.x * ca.x + r1.y * ca.y + r1.z * ca.z;
+      const float az = r2.x * ca.x + r2.y * ca.y + r2.z * ca.z;
+      const float al = sqrtf(ax * ax + ay * ay + az * az);
+      const float ux = wx - ex, uy = wy - ey, uz = wz - ez;
+      const float d = sqrtf(ux * ux + uy * uy + uz * uz);
+      if (al > 0.f && d > R) {
+        // every normal n lies within the cone's half-angle th of the axis, and the directions to the sphere's
+        // points within phi of u: dot(n, p - e) >= d cos(phi + th) - R > 0 means every triangle faces away
+        const float cphi = (ux * ax + uy * ay + uz * az) / (d * al);
+        const float sphi = sqrtf(fmaxf(0.f, 1.f - cphi * cphi));
+        const float sth = sqrtf(fmaxf(0.f, 1.f - ca.w * ca.w));
+        if (d * (cphi * ca.w - sphi * sth) > R + 1e-2f * d) return true;
+      }
+    }
+  }
+  const float cx = vp[0] * wx + vp[1] * wy + vp[2] * wz + vp[3], cy = vp[4] * wx + vp[5] * wy + vp[6] * wz + vp[7];
+  const float cw = vp[12] * wx + vp[13] * wy + vp[14] * wz + vp[15];
+  float xmin = 3.0e38f, xmax = -3.0e38f, ymin = 3.0e38f, ymax = -3.0e38f;
+  bool ok = true;
+#pragma unroll
+  for (int corner = 0; corner < 8; ++corner) {
+    const float sx = (corner & 1) ? R : -R, sy = (corner & 2) ? R : -R, sz = (corner & 4) ? R : -R;
+    const float x = cx + vp[0] * sx + vp[1] * sy + vp[2] * sz;
+    const float y = cy + vp[4] * sx + vp[5] * sy + vp[6] * sz;
+    const float w = cw + vp[12] * sx + vp[13] * sy + vp[14] * sz;
+    ok = ok && (w > 1e-6f);
+    const float iw = 1.f / w;
+    const float px = (x * iw + 1.f) * 0.5f * W, py = (1.f - y * iw) * 0.5f * H;
+    xmin = fminf(xmin, px);
+    xmax = fmaxf(xmax, px);
+    ymin = fminf(ymin, py);
+    ymax = fmaxf(ymax, py);
+    ok = ok && isfinite(px) && isfinite(py);
+  }
+  if (!ok) return false;
+  // no pixel centre i + 0.5 within [min, max] (0.01 px margin) inside the image's columns and the region's rows
+  const float ix0 = fmaxf(ceilf(xmin - 0.51f), 0.f), ix1 = fminf(floorf(xmax - 0.49f), W - 1.f);
+  const float iy0 = fmaxf(ceilf(ymin - 0.51f), ry0), iy1 = fminf(floorf(ymax - 0.49f), ry1);
+  return ix0 > ix1 || iy0 > iy1;
+}
 
 template <int THREADS, bool PLAIN, bool WINNER, bool TEX>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __grid_constant__ SceneParams P,
@@ -36,6 +123,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
   int* s_item = reinterpret_cast<int*>(s_vp + 16);
   uint32_t* s_keep = reinterpret_cast<uint32_t*>(s_item + 4);           // [kInstWords] kept instances of a batch
   int* s_ci = reinterpret_cast<int*>(s_keep + kInstWords);              // [kMaxInstBatch] their batch indices
+  int* s_pairs = reinterpret_cast<int*>(smem + L.pairs);  // [kMaxClusterPairs] kept (instance, cluster) pairs
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int W = P.W, H = P.H;
@@ -118,22 +206,24 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           for (int bx = ux0; bx <= ux1; ++bx) {
             const bool bit = (bx >= bx0) && (bx <= bx1) && (by >= by0) && (by <= by1);
             const uint32_t m = __ballot_sync(0xffffffffu, bit);
-            if (lane == 0) masks[(by * A.bins_x + bx) * words + w] = m;
+            if (lane == 0) masks[PBR_IX((by * A.bins_x + bx) * words + w, A.max_region_bins * words, 11)] = m;
           }
       }
       __syncthreads();
-      // bins warp-strided; per bin and mask word, the candidates' (triangle, pixel)
-      // pairs inside the bin are packed 32 per pass (prefix sum of the clipped bbox areas)
-      for (int b = warp; b < nbins; b += NW) {
-        const int bry = b / A.bins_x, bcx = b - bry * A.bins_x;
-        const int bx0 = bcx * B, bx1 = min(bx0 + B, W) - 1;
-        const int by0 = max((by_lo + bry) * B, ry0), by1 = min((by_lo + bry) * B + B - 1, ry1);
-        for (int w = 0; w < nw; ++w) {
-          const uint32_t m = masks[b * words + w];
+      // (bin, mask word) pairs warp-strided, so that a few crowded bins do not hold the other warps idle; per
+      // pair, the candidates' (triangle, pixel) pairs inside the bin are packed 32 per pass (prefix sum of the
+      // clipped bbox areas).  Fragments of different warps meet only in the atomicMin on the pixel keys.
+      for (int bw_item = warp; bw_item < nbins * nw; bw_item += NW) {
+        const int b = bw_item / nw, w = bw_item - b * nw;
+        {
+          const uint32_t m = masks[PBR_IX(b * words + w, A.max_region_bins * words, 11)];
           if (m == 0u) continue;
+          const int bry = b / A.bins_x, bcx = b - bry * A.bins_x;
+          const int bx0 = bcx * B, bx1 = min(bx0 + B, W) - 1;
+          const int by0 = max((by_lo + bry) * B, ry0), by1 = min((by_lo + bry) * B + B - 1, ry1);
           int ax0 = 0, ay0 = 0, bw = 1, npx = 0;
           if ((m >> lane) & 1u) {
-            const int t = w * 32 + lane;
+            const int t = (int)PBR_IX(w * 32 + lane, A.tri_cap, 9);
             const uint32_t xb = __float_as_uint(S.T3[t].w), yb = __float_as_uint(S.T4[t].x);
             ax0 = max((int)(xb & 0xffffu), bx0);
             const int ax1 = min((int)(xb >> 16), bx1);
@@ -166,13 +256,14 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             const int o_bw = __shfl_sync(0xffffffffu, bw, o);
             const float o_ibw = __shfl_sync(0xffffffffu, ibw, o);
             if (g >= total) continue;
-            const int t = w * 32 + o;
+            const int t = (int)PBR_IX(w * 32 + o, A.tri_cap, 9);
             const int local = g - o_start;
             // (local + 0.5) / bw lies at least 0.5 / bw >= 1/64 from an integer
             const int ry = (int)(((float)local + 0.5f) * o_ibw);
             const int xx = o_ax0 + local - ry * o_bw, yy = o_ay0 + ry;
             const int q = yy * W + xx;
             if (q < p0 || q >= p1) continue;  // the region starts or ends inside a row
+            (void)PBR_IX(q - p0, THREADS * kPx, 13);
             const float px = (float)xx + 0.5f, py = (float)yy + 0.5f;
             const float4 e0 = S.T0[t], e1 = S.T1[t], e2 = S.T2[t], zp = S.T3[t];
             const uint32_t fl = __float_as_uint(S.T4[t].y);
@@ -199,7 +290,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
       for (int j = 0; j < kPx; ++j) {
         const uint32_t lo = (uint32_t)keys[tid * kPx + j];
         if (q0 + j < p1 && lo > emit_base) {
-          const int t = (int)(lo - emit_base) - 1;
+          const int t = (int)PBR_IX((int)(lo - emit_base) - 1, A.tri_cap, 10);
           const float4 meta = S.T4[t];
           if (__float_as_uint(meta.y) & 8u) {
             int x = lx + j;
@@ -279,6 +370,38 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
     const float vp4 = s_vp[4], vp5 = s_vp[5], vp6 = s_vp[6], vp7 = s_vp[7];
     const float vp8 = s_vp[8], vp9 = s_vp[9], vp10 = s_vp[10], vp11 = s_vp[11];
     const float vp12 = s_vp[12], vp13 = s_vp[13], vp14 = s_vp[14], vp15 = s_vp[15];
+    // clip coordinates of mesh vertex vi of an instance (model rows r0..r2): one expression for every path, so
+    // that a vertex shared by a cluster's warp and the same vertex transformed per corner round alike
+    auto clip_of = [&](const MeshDesc& me, int vi, float4 r0, float4 r1, float4 r2) -> float4 {
+      vi = (int)PBR_IX(vi, me.nv, 5);
+      const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
+      const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
+      const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
+      const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
+      float4 o;
+      o.x = vp0 * wx + vp1 * wy + vp2 * wz + vp3;
+      o.y = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
+      o.z = vp8 * wx + vp9 * wy + vp10 * wz + vp11;
+      o.w = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
+      return o;
+    };
+    // The eye: the point where rows 0, 1 and 3 of the view-projection vanish (the centre of a perspective
+    // projection); for the clusters' facing test.  A singular system (no centre of projection) disables it.
+    float ex = 0.f, ey = 0.f, ez = 0.f;
+    bool eye_ok = false;
+    if (A.cl_any) {
+      const float bcx = vp5 * vp14 - vp6 * vp13, bcy = vp6 * vp12 - vp4 * vp14, bcz = vp4 * vp13 - vp5 * vp12;
+      const float cax = vp13 * vp2 - vp14 * vp1, cay = vp14 * vp0 - vp12 * vp2, caz = vp12 * vp1 - vp13 * vp0;
+      const float abx = vp1 * vp6 - vp2 * vp5, aby = vp2 * vp4 - vp0 * vp6, abz = vp0 * vp5 - vp1 * vp4;
+      const float det = vp0 * bcx + vp1 * bcy + vp2 * bcz;
+      if (fabsf(det) > 1e-20f) {
+        const float id = 1.f / det;
+        ex = (-vp3 * bcx - vp7 * cax - vp15 * abx) * id;
+        ey = (-vp3 * bcy - vp7 * cay - vp15 * aby) * id;
+        ez = (-vp3 * bcz - vp7 * caz - vp15 * abz) * id;
+        eye_ok = isfinite(ex) && isfinite(ey) && isfinite(ez);
+      }
+    }
     int parity = 0;
     for (int n = A.node_begin; n < A.node_end; ++n) {
       const NodeDesc& nd = P.nodes[n];
@@ -293,10 +416,13 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
         const int nbc = min(A.icap, cnt - b0);
         __syncthreads();  // the previous batch's triangles are done with icache
         for (int i = tid; i < nbc; i += THREADS) {
-          const long long id = nd.shared ? (long long)(b0 + i) : (long long)k * nd.ips + b0 + i;
+          const long long id =
+              PBR_IX(nd.shared ? (long long)(b0 + i) : (long long)k * nd.ips + b0 + i,
+                     nd.shared ? (long long)nd.ips : (long long)P.N * nd.ips, 12);
           float m[12];
           build_model(nd, id, m);
           if (r == 0) write_back_bound(nd, id);
+          (void)PBR_IX(i, A.icap, 1);
           icache[i * 4 + 0] = make_float4(m[0], m[1], m[2], m[3]);
           icache[i * 4 + 1] = make_float4(m[4], m[5], m[6], m[7]);
           icache[i * 4 + 2] = make_float4(m[8], m[9], m[10], m[11]);
@@ -363,13 +489,56 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             if ((word >> (i & 31)) & 1u) {
               int slot = __popc(word & ((1u << (i & 31)) - 1u));
               for (int wd = 0; wd < (i >> 5); ++wd) slot += __popc(s_keep[wd]);
-              s_ci[slot] = i;
+              s_ci[PBR_IX(slot, kMaxInstBatch, 2)] = i;
             }
           }
           nb = total_keep;
           __syncthreads();
         }
-        const int total_t = nb * nt;
+        // Meshes with clusters: the kept instances in sub-batches whose (instance, cluster) pairs fit the pair
+        // list; each pair is tested (cluster_culled) and the survivors compacted in draw order, then the
+        // triangle rounds run over the kept pairs' triangles only.  The culled clusters hold no triangle that
+        // would be drawn, so the output is the same as without clusters.
+        const bool use_cl = A.cl_any && me.clusters != nullptr && me.ncl > 0;
+        const int per_sub = use_cl ? max(1, kMaxClusterPairs / me.ncl) : max(nb, 1);
+        for (int s0 = 0; s0 < nb; s0 += per_sub) {
+        const int ns = min(per_sub, nb - s0);
+        int nkept = 0;
+        if (use_cl) {
+          __syncthreads();  // the previous sub-batch's triangles are done with the pair list
+          const float vpa[16] = {vp0, vp1, vp2, vp3, vp4, vp5, vp6, vp7, vp8, vp9, vp10, vp11, vp12, vp13, vp14, vp15};
+          for (int p0 = 0; p0 < ns * me.ncl; p0 += THREADS) {
+            const int p = p0 + tid;
+            bool keep = false;
+            int li = 0, c = 0;
+            if (p < ns * me.ncl) {
+              const int lv = p / me.ncl;
+              c = p - lv * me.ncl;
+              li = (int)PBR_IX(can_cull ? s_ci[PBR_IX(s0 + lv, kMaxInstBatch, 2)] : s0 + lv, A.icap, 1);
+              c = (int)PBR_IX(c, me.ncl, 7);
+              keep = !cluster_culled(me.clusters[2 * c], me.clusters[2 * c + 1], icache[li * 4 + 0],
+                                     icache[li * 4 + 1], icache[li * 4 + 2], vpa, ex, ey, ez, eye_ok,
+                                     nd.mode == kModeHpr, S.W, S.H, S.ry0, S.ry1);
+            }
+            const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+            int* wc = s_scan + parity * NW;
+            if (lane == 0) wc[warp] = __popc(bal);
+            __syncthreads();
+            int before = 0, total = 0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+              const int v = wc[w];
+              before += w < warp ? v : 0;
+              total += v;
+            }
+            parity ^= 1;
+            if (keep) s_pairs[PBR_IX(nkept + before + __popc(bal & ((1u << lane) - 1u)), kMaxClusterPairs, 3)] =
+                (li << 16) | c;
+            nkept += total;
+          }
+          __syncthreads();
+        }
+        const int total_t = use_cl ? nkept * kClusterTris : nb * nt;
         for (int t0 = 0; t0 < total_t; t0 += RT) {
           // up to 2 emitted triangles per source triangle (near-plane clip)
           const int rem = min(RT, total_t - t0);
@@ -378,28 +547,32 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           float4 cv[3];
           SV sv[3];
           bool front = false;
-          if (tid < rem) {
+          bool has = tid < rem;
+          if (has) {
             const int t = t0 + tid;
-            li = t / nt;
-            ti = t - li * nt;
-            if (can_cull) li = s_ci[li];
+            if (use_cl) {
+              const int pr = s_pairs[PBR_IX(t / kClusterTris, kMaxClusterPairs, 3)];
+              li = pr >> 16;
+              ti = (pr & 0xffff) * kClusterTris + (t & (kClusterTris - 1));
+              has = ti < nt;  // the mesh's last cluster may hold fewer triangles
+            } else {
+              li = t / nt;
+              ti = t - li * nt;
+              if (can_cull) li = s_ci[PBR_IX(li, kMaxInstBatch, 2)];
+            }
+            if (has) {
+              li = (int)PBR_IX(li, A.icap, 1);
+              ti = (int)PBR_IX(ti, nt, 4);
+            }
+          }
+          if (has) {
             i0 = me.idx[3 * ti];
             i1 = me.idx[3 * ti + 1];
             i2 = me.idx[3 * ti + 2];
             const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
-            const int iv[3] = {i0, i1, i2};
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              const int vi = iv[q];
-              const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
-              const float wx = r0.x * ox + r0.y * oy + r0.z * oz + r0.w;
-              const float wy = r1.x * ox + r1.y * oy + r1.z * oz + r1.w;
-              const float wz = r2.x * ox + r2.y * oy + r2.z * oz + r2.w;
-              cv[q].x = vp0 * wx + vp1 * wy + vp2 * wz + vp3;
-              cv[q].y = vp4 * wx + vp5 * wy + vp6 * wz + vp7;
-              cv[q].z = vp8 * wx + vp9 * wy + vp10 * wz + vp11;
-              cv[q].w = vp12 * wx + vp13 * wy + vp14 * wz + vp15;
-            }
+            cv[0] = clip_of(me, i0, r0, r1, r2);
+            cv[1] = clip_of(me, i1, r0, r1, r2);
+            cv[2] = clip_of(me, i2, r0, r1, r2);
             const float d0 = cv[0].z + cv[0].w, d1 = cv[1].z + cv[1].w, d2 = cv[2].z + cv[2].w;
             front = d0 >= 0.f && d1 >= 0.f && d2 >= 0.f;
             const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -430,7 +603,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           }
           parity ^= 1;
           if (c > 0) {
-            const int slot = tri_count + before + incl - c;
+            const int slot0 = tri_count + before + incl - c, last = slot0 + c - 1;
+            const int slot = (int)PBR_IX(last, A.tri_cap, 8) == last ? slot0 : 0;
             const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
             const float4 col = icache[li * 4 + 3];
             const int draw_id = (nd.rank_base + b0 + li) * P.max_tris + ti;
@@ -440,7 +614,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
               if (q == 0 || smooth) {
-                const int vi = iv[q];
+                const int vi = (int)PBR_IX(iv[q], me.nv, 6);
                 const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
                 const float nx = r0.x * ax + r0.y * ay + r0.z * az;
                 const float ny = r1.x * ax + r1.y * ay + r1.z * az;
@@ -459,14 +633,20 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
               tx.t2 = mesh_uv(me, i2);
               tx.node = n;
             }
-            if (front)
-              setup_tri_sv<true>(P, S, sv[0], nv[0], sv[1], nv[1], sv[2], nv[2], slot, col, draw_id, smooth, tx);
-            else
-              clip_tri<true>(P, S, cv[0], nv[0], cv[1], nv[1], cv[2], nv[2], i0, i1, i2, slot, col, draw_id, smooth,
-                             tx);
+            // Exactly the c slots this thread reserved are written, whatever the write pass decides: a triangle it
+            // rejects after all (the count pass and this pass are separate inlined copies of the setup) leaves an
+            // empty record, never the stale record of an earlier chunk or work item for the binner to read.
+            if (front) {
+              if (!setup_tri_sv<true>(P, S, sv[0], nv[0], sv[1], nv[1], sv[2], nv[2], slot, col, draw_id, smooth, tx))
+                write_empty(S, slot);
+            } else {
+              clip_tri<true>(P, S, cv[0], nv[0], cv[1], nv[1], cv[2], nv[2], i0, i1, i2, slot, col, draw_id, smooth, tx,
+                             c);
+            }
           }
           tri_count += total;
         }
+        }  // sub-batches
       }
     }
     flush(true);

@@ -26,6 +26,9 @@ enum : int {
   kStatusCapacity = 2,     // a chunk could not hold one round of triangles
 };
 
+constexpr int kClusterTris = 32;    // triangles per cluster (the last cluster of a mesh may hold fewer)
+constexpr int kMaxClusterPairs = 2048;  // (instance, cluster) pairs the tile kernel compacts at a time
+
 struct MeshDesc {
   const float* pos;    // [nv,3]
   const float* nrm;    // [nv,3]
@@ -33,6 +36,10 @@ struct MeshDesc {
   const float* uv;     // [nv,2] texture coordinates, or null (all 0)
   int32_t nv, nt, smooth, pad;
   float4 bound;        // bounding sphere (centre, radius) in mesh coordinates; radius <= 0: unknown
+  // clusters of kClusterTris consecutive triangles, two float4 each: bounding sphere (centre, radius) and the
+  // cone of their face normals (unit axis, cosine of its half-angle; <= 0: no cone); null: none
+  const float4* clusters;
+  int32_t ncl, pad1, pad2, pad3;
 };
 
 struct NodeDesc {
@@ -90,6 +97,7 @@ struct RasterArgs {
   int32_t smooth_any;  // per-pixel shading records S0..S3 (smooth meshes or textured nodes)
   int32_t tex_any;     // texture-coordinate records S4, S5 (textured nodes)
   int32_t multi_chunk;
+  int32_t cl_any;      // some node's mesh has clusters: the tile kernel culls (instance, cluster) pairs
 };
 
 // Soft-coverage launch arguments (pbr_soft.cu).
@@ -123,6 +131,7 @@ struct SmemLayout {
   int icache;              // float4 [icap*4]: model matrix rows, colour
   int state;               // per-pixel depth / emit-order keys of the region [threads*kPx] (uint64)
   int misc;                // per-warp survivor counts (two rounds), VP, work item, instance compaction
+  int pairs;               // kept (instance, cluster) pairs [kMaxClusterPairs] and the scene's eye (float4)
   int total;
 };
 
@@ -157,6 +166,7 @@ __host__ __device__ inline SmemLayout smem_layout(const RasterArgs& a, int threa
   L.state = off;  // depth / emit-order keys of the region's pixels, uint64 each
   off += align16(threads * kPx * 8);
   L.misc = off; off += align16((2 * (threads / 32) + 8) * 4 + 16 * 4 + 16 + (kInstWords + kMaxInstBatch) * 4);
+  L.pairs = off; off += a.cl_any ? align16(kMaxClusterPairs * 4 + 16) : 0;  // kept pairs; eye position
   L.total = off;
   return L;
 }

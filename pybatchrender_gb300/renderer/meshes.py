@@ -83,6 +83,42 @@ class Mesh:
         r = float(np.sqrt(((p - c) ** 2).sum(axis=1)).max())
         return (float(c[0]), float(c[1]), float(c[2])), r * (1.0 + 1e-5) + 1e-7
 
+    CLUSTER_TRIANGLES = 32
+
+    def clusters(self) -> np.ndarray:
+        """Per group of 32 consecutive triangles (the last one may hold fewer),
+        8 float32: the group's bounding sphere (centre, radius) and the cone of
+        its triangles' geometric normals (unit axis, cosine of the half-angle;
+        -1 when the normals span a half-space or more).  Both are widened
+        slightly (radius by a relative 1e-5, the half-angle by 1e-4 in its
+        cosine), so that the float32 values still bound the float64 ones."""
+        ct = self.CLUSTER_TRIANGLES
+        nt = self.num_triangles
+        ncl = (nt + ct - 1) // ct
+        out = np.zeros((ncl, 8), np.float32)
+        p = self.positions.astype(np.float64)
+        f = self.indices.astype(np.int64)
+        fn = np.cross(p[f[:, 1]] - p[f[:, 0]], p[f[:, 2]] - p[f[:, 0]])
+        fl = np.linalg.norm(fn, axis=1)
+        valid = fl > 0
+        n = np.zeros_like(fn)
+        n[valid] = fn[valid] / fl[valid, None]
+        for c in range(ncl):
+            sl = slice(c * ct, min((c + 1) * ct, nt))
+            pts = p[np.unique(f[sl].ravel())]
+            ctr = (pts.min(axis=0) + pts.max(axis=0)) * 0.5
+            r = float(np.sqrt(((pts - ctr) ** 2).sum(axis=1)).max()) * (1.0 + 1e-5) + 1e-7
+            ns = n[sl][valid[sl]]
+            axis, cos_t = np.array([0.0, 0.0, 1.0]), -1.0
+            if len(ns):
+                a = ns.sum(axis=0)
+                al = float(np.linalg.norm(a))
+                if al > 1e-9:
+                    axis = a / al
+                    cos_t = float((ns @ axis).min()) - 1e-4
+            out[c] = (*ctr, r, *axis, cos_t if cos_t > 0.0 else -1.0)
+        return out
+
     def copy(self) -> "Mesh":
         return Mesh(self.positions.copy(), self.normals.copy(), self.indices.copy(), self.name,
                     uvs=None if self.uvs is None else self.uvs.copy(), texture=self.texture)

@@ -531,6 +531,11 @@ class PBRRenderer:
                                m.num_vertices, m.num_triangles, int(m.smooth), ctypes.byref(mid))
                     c, rad = m.bounding_sphere()
                     _capi.call(lib, ctx, "pbr_mesh_set_bounds", mid.value, *c, rad)
+                    if self.cfg.cluster_cull and m.num_triangles >= 128:
+                        cl = torch.from_numpy(m.clusters()).to(self.device)
+                        self._mesh_tensors.append((cl,))
+                        _capi.call(lib, ctx, "pbr_mesh_set_clusters", mid.value, _capi.ptr(cl), int(cl.shape[0]),
+                                   m.CLUSTER_TRIANGLES)
                     if m.uvs is not None:
                         uv = torch.from_numpy(m.uvs).to(self.device)
                         self._mesh_tensors.append((uv,))

@@ -225,3 +225,25 @@ def test_report_fps_prints(capsys):
     q = pbr.PBRRenderer(num_scenes=10, device="cpu", report_fps=False)
     q.step(return_pixels=False)
     assert capsys.readouterr().out == ""
+
+
+def test_mesh_clusters_bound_their_triangles():
+    """Mesh.clusters(): each group of 32 consecutive triangles lies inside its
+    bounding sphere, and every (non-degenerate) geometric face normal of the
+    group lies inside its normal cone."""
+    import numpy as np
+    from pybatchrender_gb300.renderer import meshes
+    for m in (meshes.icosphere(3), meshes.icosphere(2), meshes.cylinder(64), meshes.unit_cube()):
+        cl = m.clusters().astype(np.float64)
+        assert cl.shape == ((m.num_triangles + 31) // 32, 8)
+        p = m.positions.astype(np.float64)
+        f = m.indices
+        fn = np.cross(p[f[:, 1]] - p[f[:, 0]], p[f[:, 2]] - p[f[:, 0]])
+        for c in range(cl.shape[0]):
+            sl = slice(32 * c, min(32 * (c + 1), m.num_triangles))
+            pts = p[f[sl].ravel()]
+            assert np.linalg.norm(pts - cl[c, :3], axis=1).max() <= cl[c, 3]
+            if cl[c, 7] > 0:
+                n = fn[sl] / np.linalg.norm(fn[sl], axis=1, keepdims=True)
+                assert (n @ cl[c, 4:7]).min() >= cl[c, 7]
+

@@ -25,6 +25,8 @@ struct pbr_ctx {
   int device = 0;
   int sm_count = 1;
   int max_smem = 48 * 1024;
+  int smem_per_sm = 0;       // shared memory of an SM, and what each resident block reserves of it
+  int smem_reserved = 0;
   std::string err;
   SceneParams P;
   std::vector<bool> node_ready;
@@ -176,6 +178,23 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
                    "scene does not fit in shared memory (%d bytes needed, %d available); "
                    "reduce mesh size or threads", L.total, ctx->max_smem);
   }
+  // A smaller instance batch (down to 64) when that lets more blocks share an SM: its shared memory is the
+  // usual limit (register use allows 2 blocks of 256 threads).
+  if (ctx->smem_per_sm > 0) {
+    auto blocks = [&](int bytes) { return ctx->smem_per_sm / (bytes + ctx->smem_reserved); };
+    int best_icap = A.icap, best_smem = out->smem;
+    for (int ic = A.icap / 2; ic >= 64; ic /= 2) {
+      RasterArgs B = A;
+      B.icap = ic;
+      const int bytes = pbr::smem_layout(B, threads, winner).total;
+      if (blocks(bytes) > blocks(best_smem)) {
+        best_icap = ic;
+        best_smem = bytes;
+      }
+    }
+    A.icap = best_icap;
+    out->smem = best_smem;
+  }
   // kernel attribute + occupancy
   int& cached = ctx->smem_set[threads_index(threads)][plain ? 1 : 0][winner ? 1 : 0][A.tex_any ? 1 : 0];
   if (out->smem > 48 * 1024 && out->smem > cached) {
@@ -313,6 +332,8 @@ int pbr_create(pbr_ctx** out_ctx, int num_scenes, int width, int height, int cha
   }
   cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
   cudaDeviceGetAttribute(&ctx->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+  cudaDeviceGetAttribute(&ctx->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device);
+  cudaDeviceGetAttribute(&ctx->smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock, ctx->device);
   ctx->P.N = num_scenes;
   ctx->P.W = width;
   ctx->P.H = height;
@@ -633,7 +654,7 @@ int pbr_autotune(pbr_ctx* ctx, uint8_t* d_out, void* stream, int* out_kernel, in
     }
     const long long need = 2 * scene_source_tris(ctx, 0, ctx->P.num_nodes);
     std::vector<int> caps = {0};
-    if (need > 256) { caps.push_back(256); caps.push_back(512); }
+    if (need > 256) { caps.push_back(256); caps.push_back(384); caps.push_back(512); }
     for (int t : {128, 256, 512})
       for (int b : {8, 16, 32})
         for (int p : {0, 1})

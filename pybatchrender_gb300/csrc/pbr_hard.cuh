@@ -540,9 +540,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
         }
         const int total_t = use_cl ? nkept * kClusterTris : nb * nt;
         for (int t0 = 0; t0 < total_t; t0 += RT) {
-          // up to 2 emitted triangles per source triangle (near-plane clip)
           const int rem = min(RT, total_t - t0);
-          if (tri_count + 2 * rem > A.tri_cap) flush(false);
           int c = 0, li = 0, ti = 0, i0 = 0, i1 = 0, i2 = 0;
           float4 cv[3];
           SV sv[3];
@@ -602,6 +600,10 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             total += v;
           }
           parity ^= 1;
+          // A round emits at most 2 triangles per source triangle (near-plane clip), so total <= 2 * RT <= tri_cap:
+          // the chunk is flushed only when this round's kept triangles do not fit; they keep their setup inputs in
+          // registers across the flush.
+          if (tri_count + total > A.tri_cap) flush(false);
           if (c > 0) {
             const int slot0 = tri_count + before + incl - c, last = slot0 + c - 1;
             const int slot = (int)PBR_IX(last, A.tri_cap, 8) == last ? slot0 : 0;

@@ -151,6 +151,9 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
   for (int n = n0; n < n1; ++n) icap = std::max(icap, P.nodes[n].ips);
   A.icap = std::min(icap, 256);
   const long long need = 2 * scene_source_tris(ctx, n0, n1);
+  // the coverage-and-depth pre-test pays where scenes hold at least as many source triangles as pixels (many
+  // small, overlapping triangles); in sparser scenes it costs more than it saves
+  A.win_test = need / 2 >= (long long)HW ? 1 : 0;
   int cap = tri_cap_req > 0 ? tri_cap_req : (int)std::min<long long>(std::max<long long>(need, 64), 1024);
   cap = std::max(64, (cap + 31) & ~31);
   A.persistent = persistent;

@@ -100,8 +100,9 @@ __device__ __forceinline__ bool cluster_culled(float4 cs, float4 ca, float4 r0, 
 // so far, holds a larger depth than the triangle's at that centre.  A triangle
 // emitted later wins a pixel only with a strictly smaller depth, and the
 // arithmetic is the setup's and the raster's, so the triangles this drops
-// would not have changed any pixel.  Triangles whose box holds more than 4
-// pixel centres are kept untested.
+// would not have changed any pixel.  The depth plane (and its division) is
+// formed only once a centre is found covered.  Triangles whose box holds more
+// than 16 pixel centres are kept untested.
 __device__ __forceinline__ bool may_win(const SetupCtx& S, SV v0, SV v1, SV v2,
                                         const unsigned long long* keys, int W, int p0, int p1) {
   float area2 = fmaf(v1.x - v0.x, v2.y - v0.y, -((v2.x - v0.x) * (v1.y - v0.y)));
@@ -114,15 +115,13 @@ __device__ __forceinline__ bool may_win(const SetupCtx& S, SV v0, SV v1, SV v2,
   const float fx0 = fmaxf(ceilf(mnx - 0.501f), 0.f), fx1 = fminf(floorf(mxx - 0.499f), S.W - 1.f);
   const float fy0 = fmaxf(ceilf(mny - 0.501f), S.ry0), fy1 = fminf(floorf(mxy - 0.499f), S.ry1);
   const int x0 = (int)fx0, x1 = (int)fx1, y0 = (int)fy0, y1 = (int)fy1;
-  if ((x1 - x0 + 1) * (y1 - y0 + 1) > 4) return true;
+  if ((x1 - x0 + 1) * (y1 - y0 + 1) > 16) return true;
   bool tl0, tl1, tl2;
   const float4 e0 = make_edge(v1.x, v1.y, v2.x, v2.y, tl0);
   const float4 e1 = make_edge(v2.x, v2.y, v0.x, v0.y, tl1);
   const float4 e2 = make_edge(v0.x, v0.y, v1.x, v1.y, tl2);
-  const float ia = 1.f / area2;
-  const float zA = fmaf(e2.x, v2.z, fmaf(e1.x, v1.z, e0.x * v0.z)) * ia;
-  const float zB = fmaf(e2.y, v2.z, fmaf(e1.y, v1.z, e0.y * v0.z)) * ia;
-  const float zC = fmaf(-zB, v0.y, fmaf(-zA, v0.x, v0.z));
+  bool plane = false;
+  float zA = 0.f, zB = 0.f, zC = 0.f;
   for (int yy = y0; yy <= y1; ++yy)
     for (int xx = x0; xx <= x1; ++xx) {
       const int q = yy * W + xx;
@@ -135,6 +134,13 @@ __device__ __forceinline__ bool may_win(const SetupCtx& S, SV v0, SV v1, SV v2,
       const bool in1 = tl1 ? (E1 >= 0.f) : (E1 > 0.f);
       const bool in2 = tl2 ? (E2 >= 0.f) : (E2 > 0.f);
       if (in0 && in1 && in2) {
+        if (!plane) {
+          const float ia = 1.f / area2;
+          zA = fmaf(e2.x, v2.z, fmaf(e1.x, v1.z, e0.x * v0.z)) * ia;
+          zB = fmaf(e2.y, v2.z, fmaf(e1.y, v1.z, e0.y * v0.z)) * ia;
+          zC = fmaf(-zB, v0.y, fmaf(-zA, v0.x, v0.z));
+          plane = true;
+        }
         const float z = fmaxf(fmaf(zA, px, fmaf(zB, py, zC)), 0.f);
         if ((__float_as_uint(z) & 0x7fffffffu) < (uint32_t)(keys[q - p0] >> 32)) return true;
       }
@@ -626,7 +632,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
 #pragma unroll
               for (int q = 0; q < 3; ++q) sv[q] = to_screen(cv[q], S.W, S.H);
               c = setup_tri_sv<false>(P, S, sv[0], z4, sv[1], z4, sv[2], z4, 0, z4, 0, smooth);
-              if (c && !may_win(S, sv[0], sv[1], sv[2], keys, W, p0, p1)) c = 0;
+              if (c && A.win_test && !may_win(S, sv[0], sv[1], sv[2], keys, W, p0, p1)) c = 0;
             } else if (!(d0 < 0.f && d1 < 0.f && d2 < 0.f)) {
               c = clip_tri<false>(P, S, cv[0], z4, cv[1], z4, cv[2], z4, i0, i1, i2, 0, z4, 0, smooth);
             }

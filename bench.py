@@ -455,6 +455,10 @@ def run_workload(args, world, rank, local):
     free0, _ = torch.cuda.mem_get_info(device)
     if name in ("many_cubes", "uneven"):
         ns = {"num_scenes": args.workload_scenes} if args.workload_scenes > 0 else {}
+        # a fixed tile-kernel launch (for profiling one configuration; the autotuner still runs unless disabled)
+        for opt, field in (("raster_threads", "raster_threads"), ("bin_size", "bin_size"), ("tri_cap", "tri_cap")):
+            if getattr(args, opt):
+                ns[field] = getattr(args, opt)
         if name == "many_cubes":
             r = workloads.many_cubes(seed=rank, return_depth=True, reuse_output=True, **ns)
             n_inst = 64.0
@@ -570,6 +574,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--workload-scenes", type=int, default=0,
                     help="scene count for --workload (0: the configuration's own; smaller for profiling)")
+    ap.add_argument("--raster-threads", type=int, default=0, help="many_cubes/uneven: tile kernel threads per CTA")
+    ap.add_argument("--bin-size", type=int, default=0, help="many_cubes/uneven: tile kernel bin size in pixels")
+    ap.add_argument("--tri-cap", type=int, default=0, help="many_cubes/uneven: tile kernel chunk size in triangles")
     ap.add_argument("--workload", default="cartpole",
                     choices=["cartpole", "many_cubes", "uneven", "soft_cartpole", "soft_large"],
                     help="cartpole = the headline; the others print their own line (see run_workload)")

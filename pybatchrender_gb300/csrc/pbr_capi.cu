@@ -147,6 +147,8 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
   A.vcap = 0;
   for (int n = n0; n < n1; ++n)
     if (P.meshes[P.nodes[n].mesh].clusters) A.cl_any = 1;
+  for (int n = n0; n < n1; ++n)
+    if (P.meshes[P.nodes[n].mesh].nt >= pbr::kMvpMinTris) A.mvp_any = 1;
   int icap = 1;
   for (int n = n0; n < n1; ++n) icap = std::max(icap, P.nodes[n].ips);
   A.icap = std::min(icap, 256);

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
   const int words = A.tri_cap >> 5;
   const int B = A.bin_px;
   const int RT = min(THREADS, A.tri_cap >> 1);
+  const int IS = A.mvp_any ? 8 : 4;  // float4 per cached instance: model rows, colour [, view-projection x model rows]
 
   for (int it = 0;; ++it) {
     int item;
@@ -466,6 +467,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
       if (cnt == 0 || nt == 0) continue;
       const bool textured = TEX && nd.tex != nullptr;  // textured triangles are shaded per pixel
       const bool smooth = me.smooth != 0 || textured;
+      // meshes of kMvpMinTris+ triangles transform their vertices with the instance's VP * M in one step
+      const bool use_mvp = A.mvp_any && nt >= kMvpMinTris;
       for (int b0 = 0; b0 < cnt; b0 += A.icap) {
         const int nbc = min(A.icap, cnt - b0);
         __syncthreads();  // the previous batch's triangles are done with icache
@@ -477,11 +480,23 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           build_model(nd, id, m);
           if (r == 0) write_back_bound(nd, id);
           (void)PBR_IX(i, A.icap, 1);
-          icache[i * 4 + 0] = make_float4(m[0], m[1], m[2], m[3]);
-          icache[i * 4 + 1] = make_float4(m[4], m[5], m[6], m[7]);
-          icache[i * 4 + 2] = make_float4(m[8], m[9], m[10], m[11]);
+          icache[i * IS + 0] = make_float4(m[0], m[1], m[2], m[3]);
+          icache[i * IS + 1] = make_float4(m[4], m[5], m[6], m[7]);
+          icache[i * IS + 2] = make_float4(m[8], m[9], m[10], m[11]);
           const float* cc = nd.color + id * 4;
-          icache[i * 4 + 3] = make_float4(cc[0], cc[1], cc[2], cc[3]);
+          icache[i * IS + 3] = make_float4(cc[0], cc[1], cc[2], cc[3]);
+          if (use_mvp) {
+            // rows of VP * M (M's last row 0 0 0 1), so that a vertex takes 12 FMAs to clip space
+            const float vpr[16] = {vp0, vp1, vp2, vp3, vp4, vp5, vp6, vp7, vp8, vp9, vp10, vp11, vp12, vp13, vp14, vp15};
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+              const float a0 = vpr[4 * rr], a1 = vpr[4 * rr + 1], a2 = vpr[4 * rr + 2], a3 = vpr[4 * rr + 3];
+              icache[i * IS + 4 + rr] = make_float4(fmaf(a2, m[8], fmaf(a1, m[4], a0 * m[0])),
+                                                    fmaf(a2, m[9], fmaf(a1, m[5], a0 * m[1])),
+                                                    fmaf(a2, m[10], fmaf(a1, m[6], a0 * m[2])),
+                                                    fmaf(a2, m[11], fmaf(a1, m[7], fmaf(a0, m[3], a3))));
+            }
+          }
         }
         __syncthreads();
         // Instances whose bounding sphere projects entirely above or below this region's rows,
@@ -496,7 +511,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             const int i = i0c + tid;
             bool keep = false;
             if (i < nbc) {
-              const float4 r0 = icache[i * 4 + 0], r1 = icache[i * 4 + 1], r2 = icache[i * 4 + 2];
+              const float4 r0 = icache[i * IS + 0], r1 = icache[i * IS + 1], r2 = icache[i * IS + 2];
               const float4 b = me.bound;
               const float wx = r0.x * b.x + r0.y * b.y + r0.z * b.z + r0.w;
               const float wy = r1.x * b.x + r1.y * b.y + r1.z * b.z + r1.w;
@@ -570,8 +585,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
               c = p - lv * me.ncl;
               li = (int)PBR_IX(can_cull ? s_ci[PBR_IX(s0 + lv, kMaxInstBatch, 2)] : s0 + lv, A.icap, 1);
               c = (int)PBR_IX(c, me.ncl, 7);
-              keep = !cluster_culled(me.clusters[2 * c], me.clusters[2 * c + 1], icache[li * 4 + 0],
-                                     icache[li * 4 + 1], icache[li * 4 + 2], vpa, ex, ey, ez, eye_ok,
+              keep = !cluster_culled(me.clusters[2 * c], me.clusters[2 * c + 1], icache[li * IS + 0],
+                                     icache[li * IS + 1], icache[li * IS + 2], vpa, ex, ey, ez, eye_ok,
                                      nd.mode == kModeHpr, S.W, S.H, S.ry0, S.ry1);
             }
             const uint32_t bal = __ballot_sync(0xffffffffu, keep);
@@ -621,10 +636,25 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             i0 = me.idx[3 * ti];
             i1 = me.idx[3 * ti + 1];
             i2 = me.idx[3 * ti + 2];
-            const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
-            cv[0] = clip_of(me, i0, r0, r1, r2);
-            cv[1] = clip_of(me, i1, r0, r1, r2);
-            cv[2] = clip_of(me, i2, r0, r1, r2);
+            if (use_mvp) {
+              const float4 m0 = icache[li * IS + 4], m1 = icache[li * IS + 5], m2 = icache[li * IS + 6];
+              const float4 m3 = icache[li * IS + 7];
+              const int iv[3] = {i0, i1, i2};
+#pragma unroll
+              for (int q = 0; q < 3; ++q) {
+                const int vi = (int)PBR_IX(iv[q], me.nv, 5);
+                const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
+                cv[q] = make_float4(fmaf(m0.x, ox, fmaf(m0.y, oy, fmaf(m0.z, oz, m0.w))),
+                                    fmaf(m1.x, ox, fmaf(m1.y, oy, fmaf(m1.z, oz, m1.w))),
+                                    fmaf(m2.x, ox, fmaf(m2.y, oy, fmaf(m2.z, oz, m2.w))),
+                                    fmaf(m3.x, ox, fmaf(m3.y, oy, fmaf(m3.z, oz, m3.w))));
+              }
+            } else {
+              const float4 r0 = icache[li * IS + 0], r1 = icache[li * IS + 1], r2 = icache[li * IS + 2];
+              cv[0] = clip_of(me, i0, r0, r1, r2);
+              cv[1] = clip_of(me, i1, r0, r1, r2);
+              cv[2] = clip_of(me, i2, r0, r1, r2);
+            }
             const float d0 = cv[0].z + cv[0].w, d1 = cv[1].z + cv[1].w, d2 = cv[2].z + cv[2].w;
             front = d0 >= 0.f && d1 >= 0.f && d2 >= 0.f;
             const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -662,8 +692,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           if (c > 0) {
             const int slot0 = tri_count + before + incl - c, last = slot0 + c - 1;
             const int slot = (int)PBR_IX(last, A.tri_cap, 8) == last ? slot0 : 0;
-            const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
-            const float4 col = icache[li * 4 + 3];
+            const float4 r0 = icache[li * IS + 0], r1 = icache[li * IS + 1], r2 = icache[li * IS + 2];
+            const float4 col = icache[li * IS + 3];
             const int draw_id = (nd.rank_base + b0 + li) * P.max_tris + ti;
             // world normals: the provoking vertex's for flat meshes (the three are identical), all three if smooth
             float4 nv[3];

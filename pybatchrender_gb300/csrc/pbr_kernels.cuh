@@ -27,7 +27,8 @@ enum : int {
 };
 
 constexpr int kClusterTris = 32;    // triangles per cluster (the last cluster of a mesh may hold fewer)
-constexpr int kMaxClusterPairs = 2048;  // (instance, cluster) pairs the tile kernel compacts at a time
+constexpr int kMaxClusterPairs = 2048;
+constexpr int kMvpMinTris = 128;  // tile kernel: meshes this large transform vertices with a per-instance VP * M  // (instance, cluster) pairs the tile kernel compacts at a time
 
 struct MeshDesc {
   const float* pos;    // [nv,3]
@@ -98,7 +99,8 @@ struct RasterArgs {
   int32_t tex_any;     // texture-coordinate records S4, S5 (textured nodes)
   int32_t multi_chunk;
   int32_t cl_any;
-  int32_t win_test;  // tile kernel: pre-test small kept triangles against coverage and the keys (may_win)      // some node's mesh has clusters: the tile kernel culls (instance, cluster) pairs
+  int32_t win_test;
+  int32_t mvp_any;   // tile kernel: some node's mesh has kMvpMinTris+ triangles (instances cache VP * M too)  // tile kernel: pre-test small kept triangles against coverage and the keys (may_win)      // some node's mesh has clusters: the tile kernel culls (instance, cluster) pairs
 };
 
 // Soft-coverage launch arguments (pbr_soft.cu).
@@ -163,7 +165,7 @@ __host__ __device__ inline SmemLayout smem_layout(const RasterArgs& a, int threa
   }
   L.masks = off; off += align16(a.max_region_bins * (a.tri_cap / 32) * 4);
   L.vcache = off; off += align16(a.vcap * 32);
-  L.icache = off; off += align16(a.icap * 64);
+  L.icache = off; off += align16(a.icap * (a.mvp_any ? 128 : 64));
   L.state = off;  // depth / emit-order keys of the region's pixels, uint64 each
   off += align16(threads * kPx * 8);
   L.misc = off; off += align16((2 * (threads / 32) + 8) * 4 + 16 * 4 + 16 + (kInstWords + kMaxInstBatch) * 4);

@@ -75,3 +75,31 @@ def test_noalloc_leaves_device_memory_unchanged(cuda):
     free_after, _ = torch.cuda.mem_get_info()
     assert free_after == free_before, (free_before, free_after)
     assert torch.equal(out, first)
+
+
+def test_noalloc_inside_cuda_graph_capture(cuda):
+    """The entry point's main use: captured inside a CUDA stream capture (one
+    eager call first loads the module that holds the static scratch), then
+    replayed after the scene state changed in place; each replay equals the
+    plain path on that state."""
+    r = workloads.cartpole_bench(num_scenes=96, res=64, seed=46)
+    r._step(workloads.cartpole_states(96, seed=47, device=cuda))
+    out = torch.empty((96, 3, 64, 64), dtype=torch.uint8, device=cuda)
+    depth = torch.empty((96, 64, 64), dtype=torch.float32, device=cuda)
+    _capi.call(r._lib, r._ctx, "pbr_plain_render_noalloc", _capi.ptr(out), _capi.ptr(depth),
+               torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        _capi.call(r._lib, r._ctx, "pbr_plain_render_noalloc", _capi.ptr(out), _capi.ptr(depth),
+                   torch.cuda.current_stream().cuda_stream)
+    stream = torch.cuda.current_stream().cuda_stream
+    for seed in (48, 49):
+        r._step(workloads.cartpole_states(96, seed=seed, device=cuda))
+        g.replay()
+        ref_out = torch.empty_like(out)
+        ref_depth = torch.empty_like(depth)
+        _plain_reference(r, ref_out, ref_depth, stream)
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref_out), seed
+        assert torch.equal(depth, ref_depth), seed

@@ -94,18 +94,24 @@ __device__ __forceinline__ bool cluster_culled(float4 cs, float4 ca, float4 r0, 
   return ix0 > ix1 || iy0 > iy1;
 }
 
-// Whether a front triangle that passed the box test of setup_tri_sv can still
-// take a pixel of the region [p0, p1): it covers a pixel centre there (the
-// raster's edge functions and top-left rule) whose key, from the chunks drawn
-// so far, holds a larger depth than the triangle's at that centre.  A triangle
-// emitted later wins a pixel only with a strictly smaller depth, and the
-// arithmetic is the setup's and the raster's, so the triangles this drops
+// The count pass for a front triangle in scenes with many small triangles:
+// the tests of setup_tri_sv (orientation, box with a pixel centre of the
+// region), then, for boxes of at most 16 pixel centres, whether the triangle
+// can still take a pixel of the region [p0, p1): it covers a pixel centre there
+// (the raster's edge functions and top-left rule) whose key, from the chunks
+// drawn so far, holds a larger depth than the triangle's at that centre.  A
+// triangle emitted later wins a pixel only with a strictly smaller depth, and
+// the arithmetic is the setup's and the raster's, so the triangles this drops
 // would not have changed any pixel.  The depth plane (and its division) is
-// formed only once a centre is found covered.  Triangles whose box holds more
-// than 16 pixel centres are kept untested.
-__device__ __forceinline__ bool may_win(const SetupCtx& S, SV v0, SV v1, SV v2,
-                                        const unsigned long long* keys, int W, int p0, int p1) {
+// formed only once a centre is found covered.  Returns 1 to keep, 0 to drop.
+__device__ __forceinline__ int count_may_win(const SetupCtx& S, SV v0, SV v1, SV v2,
+                                             const unsigned long long* keys, int W, int p0, int p1) {
   float area2 = fmaf(v1.x - v0.x, v2.y - v0.y, -((v2.x - v0.x) * (v1.y - v0.y)));
+  if (S.cull) {
+    if (!(area2 < 0.f)) return 0;  // back-facing, degenerate or NaN
+  } else {
+    if (!(area2 < 0.f) && !(area2 > 0.f)) return 0;
+  }
   if (area2 < 0.f) {
     SV t = v1; v1 = v2; v2 = t;
     area2 = -area2;
@@ -114,8 +120,9 @@ __device__ __forceinline__ bool may_win(const SetupCtx& S, SV v0, SV v1, SV v2,
   const float mny = fminf(fminf(v0.y, v1.y), v2.y), mxy = fmaxf(fmaxf(v0.y, v1.y), v2.y);
   const float fx0 = fmaxf(ceilf(mnx - 0.501f), 0.f), fx1 = fminf(floorf(mxx - 0.499f), S.W - 1.f);
   const float fy0 = fmaxf(ceilf(mny - 0.501f), S.ry0), fy1 = fminf(floorf(mxy - 0.499f), S.ry1);
+  if (!(fx0 <= fx1 && fy0 <= fy1)) return 0;
   const int x0 = (int)fx0, x1 = (int)fx1, y0 = (int)fy0, y1 = (int)fy1;
-  if ((x1 - x0 + 1) * (y1 - y0 + 1) > 16) return true;
+  if ((x1 - x0 + 1) * (y1 - y0 + 1) > 16) return 1;
   bool tl0, tl1, tl2;
   const float4 e0 = make_edge(v1.x, v1.y, v2.x, v2.y, tl0);
   const float4 e1 = make_edge(v2.x, v2.y, v0.x, v0.y, tl1);
@@ -142,10 +149,10 @@ __device__ __forceinline__ bool may_win(const SetupCtx& S, SV v0, SV v1, SV v2,
           plane = true;
         }
         const float z = fmaxf(fmaf(zA, px, fmaf(zB, py, zC)), 0.f);
-        if ((__float_as_uint(z) & 0x7fffffffu) < (uint32_t)(keys[q - p0] >> 32)) return true;
+        if ((__float_as_uint(z) & 0x7fffffffu) < (uint32_t)(keys[q - p0] >> 32)) return 1;
       }
     }
-  return false;
+  return 0;
 }
 
 template <int THREADS, bool PLAIN, bool WINNER, bool TEX>
@@ -661,8 +668,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             if (front) {
 #pragma unroll
               for (int q = 0; q < 3; ++q) sv[q] = to_screen(cv[q], S.W, S.H);
-              c = setup_tri_sv<false>(P, S, sv[0], z4, sv[1], z4, sv[2], z4, 0, z4, 0, smooth);
-              if (c && A.win_test && !may_win(S, sv[0], sv[1], sv[2], keys, W, p0, p1)) c = 0;
+              c = A.win_test ? count_may_win(S, sv[0], sv[1], sv[2], keys, W, p0, p1)
+                             : setup_tri_sv<false>(P, S, sv[0], z4, sv[1], z4, sv[2], z4, 0, z4, 0, smooth);
             } else if (!(d0 < 0.f && d1 < 0.f && d2 < 0.f)) {
               c = clip_tri<false>(P, S, cv[0], z4, cv[1], z4, cv[2], z4, i0, i1, i2, 0, z4, 0, smooth);
             }

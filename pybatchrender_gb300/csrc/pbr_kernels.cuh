@@ -98,9 +98,9 @@ struct RasterArgs {
   int32_t smooth_any;  // per-pixel shading records S0..S3 (smooth meshes or textured nodes)
   int32_t tex_any;     // texture-coordinate records S4, S5 (textured nodes)
   int32_t multi_chunk;
-  int32_t cl_any;
-  int32_t win_test;
-  int32_t mvp_any;   // tile kernel: some node's mesh has kMvpMinTris+ triangles (instances cache VP * M too)  // tile kernel: pre-test small kept triangles against coverage and the keys (may_win)      // some node's mesh has clusters: the tile kernel culls (instance, cluster) pairs
+  int32_t cl_any;      // some node's mesh has clusters: the tile kernel culls (instance, cluster) pairs
+  int32_t win_test;    // tile kernel: pre-test small kept triangles against coverage and the keys (count_may_win)
+  int32_t mvp_any;     // tile kernel: some node's mesh has kMvpMinTris+ triangles (instances cache VP * M too)
 };
 
 // Soft-coverage launch arguments (pbr_soft.cu).

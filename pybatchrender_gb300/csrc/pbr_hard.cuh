@@ -674,6 +674,19 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
               c = clip_tri<false>(P, S, cv[0], z4, cv[1], z4, cv[2], z4, i0, i1, i2, 0, z4, 0, smooth);
             }
           }
+          // a kept smooth triangle's three vertex normals are loaded now, so that their latency overlaps the
+          // compaction below (a flat triangle loads its one normal in the write pass)
+          float an[9];
+          if (c > 0 && smooth) {
+            const int iv[3] = {i0, i1, i2};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const int vi = (int)PBR_IX(iv[q], me.nv, 6);
+              an[3 * q] = me.nrm[3 * vi];
+              an[3 * q + 1] = me.nrm[3 * vi + 1];
+              an[3 * q + 2] = me.nrm[3 * vi + 2];
+            }
+          }
           // draw-order compaction: warp prefix sum, then the totals of the warps before this one
           int incl = c;
 #pragma unroll
@@ -704,12 +717,20 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             const int draw_id = (nd.rank_base + b0 + li) * P.max_tris + ti;
             // world normals: the provoking vertex's for flat meshes (the three are identical), all three if smooth
             float4 nv[3];
-            const int iv[3] = {i0, i1, i2};
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
               if (q == 0 || smooth) {
-                const int vi = (int)PBR_IX(iv[q], me.nv, 6);
-                const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
+                float ax, ay, az;
+                if (smooth) {
+                  ax = an[3 * q];
+                  ay = an[3 * q + 1];
+                  az = an[3 * q + 2];
+                } else {
+                  const int vi = (int)PBR_IX(i0, me.nv, 6);
+                  ax = me.nrm[3 * vi];
+                  ay = me.nrm[3 * vi + 1];
+                  az = me.nrm[3 * vi + 2];
+                }
                 const float nx = r0.x * ax + r0.y * ay + r0.z * az;
                 const float ny = r1.x * ax + r1.y * ay + r1.z * az;
                 const float nz = r2.x * ax + r2.y * ay + r2.z * az;

@@ -306,21 +306,6 @@ __device__ __forceinline__ int clip_tri(const SceneParams& P, const SetupCtx& S,
   return cnt;
 }
 
-// One source triangle: returns the number of screen triangles emitted at
-// slot, slot+1 (0, 1, or 2 after near-plane clipping).
-template <bool WRITE>
-__device__ __forceinline__ int process_tri(const SceneParams& P, const SetupCtx& S, const float4* vcache, int vbase,
-                                           int i0, int i1, int i2, int slot, float4 col, int draw_id, bool smooth) {
-  const float4 c0 = vcache[2 * (vbase + i0)], n0 = vcache[2 * (vbase + i0) + 1];
-  const float4 c1 = vcache[2 * (vbase + i1)], n1 = vcache[2 * (vbase + i1) + 1];
-  const float4 c2 = vcache[2 * (vbase + i2)], n2 = vcache[2 * (vbase + i2) + 1];
-  const float d0 = c0.z + c0.w, d1 = c1.z + c1.w, d2 = c2.z + c2.w;
-  if (d0 >= 0.f && d1 >= 0.f && d2 >= 0.f)
-    return setup_tri<WRITE>(P, S, c0, n0, c1, n1, c2, n2, slot, col, draw_id, smooth, TexIn());
-  if (d0 < 0.f && d1 < 0.f && d2 < 0.f) return 0;
-  return clip_tri<WRITE>(P, S, c0, n0, c1, n1, c2, n2, i0, i1, i2, slot, col, draw_id, smooth);
-}
-
 // GL bilinear sample with repeat wrap (the sampler Panda3D gives a loaded
 // texture: linear filtering, no mipmaps) at texture coordinates (u, v):
 // texel centres at (i + 0.5) / w, RGBA8 texels read as c / 255.  Every index

@@ -432,8 +432,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
     const float vp4 = s_vp[4], vp5 = s_vp[5], vp6 = s_vp[6], vp7 = s_vp[7];
     const float vp8 = s_vp[8], vp9 = s_vp[9], vp10 = s_vp[10], vp11 = s_vp[11];
     const float vp12 = s_vp[12], vp13 = s_vp[13], vp14 = s_vp[14], vp15 = s_vp[15];
-    // clip coordinates of mesh vertex vi of an instance (model rows r0..r2): one expression for every path, so
-    // that a vertex shared by a cluster's warp and the same vertex transformed per corner round alike
+    // clip coordinates of mesh vertex vi of an instance (model rows r0..r2): world position, then the
+    // view-projection (meshes below kMvpMinTris triangles; larger ones use the cached VP * M rows)
     auto clip_of = [&](const MeshDesc& me, int vi, float4 r0, float4 r1, float4 r2) -> float4 {
       vi = (int)PBR_IX(vi, me.nv, 5);
       const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];

@@ -172,6 +172,14 @@ int pbr_background_set(pbr_ctx* ctx, const float rgba[4]);
  * driver schedules its own work). */
 int pbr_raster_config(pbr_ctx* ctx, int kernel, int threads, int bin_px, int tri_cap, int persistent);
 
+/* The tile kernel's pre-test of small kept triangles: a triangle whose box
+ * holds at most 16 pixel centres is kept only if it covers one of them with a
+ * depth below the key the chunks drawn so far left there.  The pixels are the
+ * same either way; it pays in scenes with many small overlapping triangles.
+ * mode -1 (the default): on when a scene holds at least as many source
+ * triangles as pixels; 0 off; 1 on.  No reference counterpart. */
+int pbr_tile_pretest(pbr_ctx* ctx, int mode);
+
 /* Time the candidate launch configurations on the bound scene and keep the
  * fastest.  d_out is an [N,C,H,W] uint8 scratch image.  Synchronises the
  * stream; do not call during graph capture.  Reports the choice through the

@@ -44,6 +44,7 @@ SIGNATURES: dict[str, list] = {
     "pbr_light_set": [_vp, _f3, _f3, _f3, _f],
     "pbr_background_set": [_vp, _f4],
     "pbr_raster_config": [_vp, _i, _i, _i, _i, _i],
+    "pbr_tile_pretest": [_vp, _i],
     "pbr_autotune": [_vp, _vp, _vp, _pi, _pi, _pi, _pi, _pi, _pf],
     "pbr_render": [_vp, _vp, _vp, _vp, _vp],
     "pbr_node_bind_state": [_vp, _i, _i, _i],

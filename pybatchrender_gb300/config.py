@@ -76,6 +76,7 @@ class PBRConfig:
     bin_size: int = 16               # binner tile size in pixels: 8 | 16 | 32
     tri_cap: int = 0                 # triangles per shared-memory chunk (0 = automatic)
     cluster_cull: bool = True        # tile kernel: skip groups of 32 triangles that cannot be drawn (meshes of 128+)
+    tile_pretest: str = 'auto'       # tile kernel: coverage-and-depth pre-test of small triangles: 'auto' | 'on' | 'off'
     persistent: bool = False         # persistent work-stealing schedule
     autotune: bool = False           # time the launch configurations at setup_environment()
     cuda_graph: bool = False         # capture _step + render into a CUDA graph on the first step
@@ -166,6 +167,8 @@ class PBRConfig:
             raise ValueError(f"raster_method must be 'batched' or 'plain', got {self.raster_method!r}")
         if self.raster_mode not in ('hard', 'soft'):
             raise ValueError(f"raster_mode must be 'hard' or 'soft', got {self.raster_mode!r}")
+        if self.tile_pretest not in ('auto', 'on', 'off'):
+            raise ValueError(f"tile_pretest must be 'auto', 'on' or 'off', got {self.tile_pretest!r}")
         if self.raster_kernel not in ('auto', 'warp', 'tile', 'binned'):
             raise ValueError("raster_kernel must be 'auto', 'warp', 'tile' or 'binned'")
         if self.raster_threads not in (128, 256, 512) and not (self.raster_kernel == 'warp'

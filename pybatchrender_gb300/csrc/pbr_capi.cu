@@ -36,6 +36,7 @@ struct pbr_ctx {
   int bin_px = 16;
   int tri_cap_req = 0;
   int persistent = 0;
+  int pretest = -1;  // tile kernel's coverage-and-depth pre-test: -1 by scene density, 0 off, 1 on
   int kernel = 0;  // 0 auto, 1 scene-per-warp, 2 tile (CTA per scene region), 3 binned (soft only)
   // scratch
   int32_t* d_counter = nullptr;
@@ -155,7 +156,7 @@ static int plan_tile(pbr_ctx* ctx, int threads, int bin_px, int tri_cap_req, int
   const long long need = 2 * scene_source_tris(ctx, n0, n1);
   // the coverage-and-depth pre-test pays where scenes hold at least as many source triangles as pixels (many
   // small, overlapping triangles); in sparser scenes it costs more than it saves
-  A.win_test = need / 2 >= (long long)HW ? 1 : 0;
+  A.win_test = ctx->pretest >= 0 ? ctx->pretest : (need / 2 >= (long long)HW ? 1 : 0);
   int cap = tri_cap_req > 0 ? tri_cap_req : (int)std::min<long long>(std::max<long long>(need, 64), 1024);
   cap = std::max(64, (cap + 31) & ~31);
   A.persistent = persistent;
@@ -596,6 +597,13 @@ int pbr_raster_config(pbr_ctx* ctx, int kernel, int threads, int bin_px, int tri
   ctx->tri_cap_req = tri_cap;
   ctx->persistent = persistent ? 1 : 0;
   ctx->kernel = kernel;
+  return PBR_OK;
+}
+
+int pbr_tile_pretest(pbr_ctx* ctx, int mode) {
+  PBR_CHECK_CTX(ctx);
+  if (mode < -1 || mode > 1) return set_err(ctx, PBR_ERR_INVALID, "mode must be -1 (by density), 0 or 1 (got %d)", mode);
+  ctx->pretest = mode;
   return PBR_OK;
 }
 

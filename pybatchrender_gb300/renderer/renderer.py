@@ -555,6 +555,7 @@ class PBRRenderer:
             _capi.call(lib, ctx, "pbr_background_set", (ctypes.c_float * 4)(*self._background_color))
             _capi.call(lib, ctx, "pbr_raster_config", KERNELS[self.cfg.raster_kernel], int(self.cfg.raster_threads),
                        int(self.cfg.bin_size), int(self.cfg.tri_cap), int(bool(self.cfg.persistent)))
+            _capi.call(lib, ctx, "pbr_tile_pretest", {"auto": -1, "off": 0, "on": 1}[self.cfg.tile_pretest])
             _capi.call(lib, ctx, "pbr_soft_config", float(self.cfg.soft_sigma), float(self.cfg.soft_gamma),
                        128 if int(self.cfg.raster_threads) == 128 else 256)
 

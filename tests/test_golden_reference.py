@@ -161,7 +161,7 @@ def test_config_defaults_match_reference():
     from pybatchrender_gb300.envs.steering import SteeringConfig
     ref = json.load(open(os.path.join(GOLDEN, "ref_config_defaults.json")))
     allowed = {}
-    own = {"autotune", "bin_size", "cluster_cull", "cuda_graph", "fused_step", "persistent", "raster_kernel", "raster_method",
+    own = {"autotune", "bin_size", "cluster_cull", "tile_pretest", "cuda_graph", "fused_step", "persistent", "raster_kernel", "raster_method",
            "raster_mode", "raster_threads", "return_depth", "reuse_output", "soft_gamma", "soft_sigma", "tri_cap"}
     for name, cls in (("PBRConfig", pbr.PBRConfig), ("CartPoleConfig", CartPoleConfig),
                       ("SteeringConfig", SteeringConfig)):

@@ -111,3 +111,21 @@ def test_triangle_soup_same_with_and_without_clusters(cuda):
         res.append(_render_all(r))
     _assert_same(*res)
     assert (res[0][2] >= 0).float().mean() > 0.05
+
+
+@pytest.mark.parametrize("scenes", ["uneven", "many_cubes"])
+def test_pretest_leaves_pixels_unchanged(cuda, scenes):
+    """The tile kernel's coverage-and-depth pre-test drops only triangles that
+    would not change a pixel: rendering with it forced on and forced off gives
+    bit-identical pixels, depth and winners, on dense uneven scenes (where it is
+    on by default) and on the many-cubes scenes (where it is off)."""
+    res = []
+    for mode in ("on", "off"):
+        if scenes == "uneven":
+            r = workloads.uneven(num_scenes=96, res=84, max_instances=256, seed=11, raster_kernel="tile",
+                                 tile_pretest=mode)
+        else:
+            r = workloads.many_cubes(num_scenes=48, seed=12, raster_kernel="tile", tile_pretest=mode)
+        res.append(_render_all(r))
+    _assert_same(*res)
+    assert (res[0][2] >= 0).float().mean() > 0.05

@@ -443,10 +443,14 @@ def run_ours(args, world, rank, local):
         fps, n, elapsed = cpu_port_fps(N, res, 0, args.cpu_budget, threads)
         line["cpu_baseline"] = {"value": fps, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{n} full steps of {N} scenes in {elapsed:.1f}s (oracle FP32 rasteriser)"}
+    if args.workloads and world == 1:
+        del graph_r, eager_r, plain_r, copy_r
+        torch.cuda.empty_cache()
+        line["workloads"] = run_workloads_inline(args, world, rank, local)
     print(json.dumps(line), flush=True)
 
 
-def run_workload(args, world, rank, local):
+def run_workload(args, world, rank, local, name: str | None = None, emit: bool = True) -> dict:
     """One of the other configurations, on its own JSON line (not the headline):
     many_cubes (1024 scenes 128x128 RGB + depth, 64 cubes), uneven (4096 scenes
     84x84, 1..512 instances of mixed meshes, graph-captured step with in-place
@@ -459,7 +463,7 @@ def run_workload(args, world, rank, local):
     _capi.load(build_if_missing=True)
     stream = torch.cuda.current_stream(device)
     flush = l2_flusher(device)
-    name = args.workload
+    name = name or args.workload
     hbm_peak, peak_src = measured_peak()
     line = {"workload": name, "unit": UNIT, "n_gpus": world, "higher_is_better": True, "scaling": "weak",
             "data": "synthetic", "steps": args.steps, "warmup": args.warmup}
@@ -572,8 +576,36 @@ def run_workload(args, world, rank, local):
     free1, _ = torch.cuda.mem_get_info(device)
     line["hbm_footprint_bytes"] = int(free0 - free1)
     line["torch_peak_allocated_bytes"] = int(torch.cuda.max_memory_allocated(device))
-    if rank == 0:
+    if rank == 0 and emit:
         print(json.dumps(line), flush=True)
+    return line
+
+
+WORKLOADS = ("many_cubes", "uneven", "soft_cartpole", "soft_large")
+
+
+def run_workloads_inline(args, world, rank, local) -> dict:
+    """The other configurations measured in the same run as the headline (one GPU), each with
+    `--workload-steps` timed steps after 3 warm-up steps, summarised under the headline line's `workloads`."""
+    import copy
+
+    out = {}
+    for name in WORKLOADS:
+        a = copy.copy(args)
+        a.steps, a.warmup, a.workload_scenes = args.workload_steps, 3, 0
+        try:
+            wl = run_workload(a, world, rank, local, name=name, emit=False)
+            keep = ("metric", "value", "unit", "ms_per_step", "steps", "dtype", "forward", "fwd_over_fwd_bwd",
+                    "hbm_footprint_bytes", "torch_peak_allocated_bytes", "clocks")
+            d = {k: wl[k] for k in keep if k in wl}
+            d["config"] = {k: wl["config"][k] for k in ("workload", "launch", "step") if k in wl.get("config", {})}
+            d["roofline"] = {k: wl["roofline"][k] for k in ("bound", "achieved", "peak", "unit", "frac",
+                                                            "bytes_per_frame") if k in wl.get("roofline", {})}
+            out[name] = d
+        except Exception as e:  # a failing configuration is reported, not fatal to the headline line
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
+        torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -594,6 +626,10 @@ def main():
     ap.add_argument("--raster-threads", type=int, default=0, help="many_cubes/uneven: tile kernel threads per CTA")
     ap.add_argument("--bin-size", type=int, default=0, help="many_cubes/uneven: tile kernel bin size in pixels")
     ap.add_argument("--tri-cap", type=int, default=0, help="many_cubes/uneven: tile kernel chunk size in triangles")
+    ap.add_argument("--no-workloads", dest="workloads", action="store_false",
+                    help="headline run only: skip the other configurations' summaries")
+    ap.add_argument("--workload-steps", type=int, default=10,
+                    help="timed steps of each configuration measured inside the headline run")
     ap.add_argument("--workload", default="cartpole",
                     choices=["cartpole", "many_cubes", "uneven", "soft_cartpole", "soft_large"],
                     help="cartpole = the headline; the others print their own line (see run_workload)")

@@ -63,6 +63,15 @@ long long soft_large_slab_float4(int cap, int nblocks) {
   return 15LL * cap + (nblocks * words + 3) / 4 + (24LL * cap + 3) / 4;
 }
 
+// The next candidate's record lines, fetched into L1 while the warp evaluates
+// the current one (lane i < kSoftRecs asks for record array i, which starts
+// at slab + i * cap): the slab is
+// larger than L2 in total, and each candidate's first loads otherwise wait on
+// DRAM.  A prefetch changes no value.
+__device__ __forceinline__ void prefetch_record(const float4* slab, int cap, int t, int lane) {
+  if (lane < kSoftRecs) asm volatile("prefetch.global.L1 [%0];" ::"l"(slab + (long long)lane * cap + t));
+}
+
 template <bool BACKWARD>
 __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __grid_constant__ SceneParams P,
                                                                    const __grid_constant__ SoftArgs A) {
@@ -244,6 +253,7 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
             while (mk) {
               const int t = (w0 + j) * 32 + __ffs(mk) - 1;
               mk &= mk - 1u;
+              if (mk) prefetch_record(slab, cap, (w0 + j) * 32 + __ffs(mk) - 1, lane);
               Frag f;
               if (!active || !soft_frag(P, S, t, px, py, inv_sigma, inv_zr, f)) continue;
               if (1.f - f.D == 0.f) nz += 1.f;
@@ -337,6 +347,7 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
             while (mk) {
               const int t = (w0 + j) * 32 + __ffs(mk) - 1;
               mk &= mk - 1u;
+              if (mk) prefetch_record(slab, cap, (w0 + j) * 32 + __ffs(mk) - 1, lane);
               float acc[24];
 #pragma unroll
               for (int i = 0; i < 24; ++i) acc[i] = 0.f;

@@ -475,6 +475,8 @@ def run_workload(args, world, rank, local, name: str | None = None, emit: bool =
         for opt, field in (("raster_threads", "raster_threads"), ("bin_size", "bin_size"), ("tri_cap", "tri_cap")):
             if getattr(args, opt):
                 ns[field] = getattr(args, opt)
+        if args.raster_kernel != "auto":
+            ns["raster_kernel"] = args.raster_kernel
         if name == "many_cubes":
             r = workloads.many_cubes(seed=rank, return_depth=True, reuse_output=True, **ns)
             n_inst = 64.0
@@ -513,14 +515,16 @@ def run_workload(args, world, rank, local, name: str | None = None, emit: bool =
     else:
         if name == "soft_cartpole":
             N, res = args.workload_scenes or 512, 64
-            r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", raster_mode="soft")
+            r = workloads.cartpole_bench(num_scenes=N, res=res, seed=rank, device="cuda", raster_mode="soft",
+                                         **({} if args.raster_kernel == "auto" else {"raster_kernel": args.raster_kernel}))
             n_inst = 2
             desc = f"{N} scenes 64x64 f32 soft coverage (sigma 0.5 px edge, gamma 1e-3), CartPole bench scene"
             states = [workloads.cartpole_states(N, seed=100 + i, device=device) for i in range(16)]
             pre = lambda i: r._step(states[i % 16])
         else:
             N, res = args.workload_scenes or 16384, 128
-            r = workloads.soft_large(num_scenes=N, res=res, seed=rank)
+            r = workloads.soft_large(num_scenes=N, res=res, seed=rank,
+                                     **({} if args.raster_kernel == "auto" else {"raster_kernel": args.raster_kernel}))
             n_inst = 128
             desc = f"{N} scenes 128x128 f32 soft coverage, 128 instances/scene (64 icosphere-s2 + 64 cubes)"
             pre = lambda i: None
@@ -623,6 +627,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--workload-scenes", type=int, default=0,
                     help="scene count for --workload (0: the configuration's own; smaller for profiling)")
+    ap.add_argument("--raster-kernel", default="auto", choices=["auto", "warp", "tile", "binned"],
+                    help="--workload lines: the raster kernel (auto: the library's choice)")
     ap.add_argument("--raster-threads", type=int, default=0, help="many_cubes/uneven: tile kernel threads per CTA")
     ap.add_argument("--bin-size", type=int, default=0, help="many_cubes/uneven: tile kernel bin size in pixels")
     ap.add_argument("--tri-cap", type=int, default=0, help="many_cubes/uneven: tile kernel chunk size in triangles")

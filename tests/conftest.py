@@ -12,6 +12,26 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and libpbr.so built for sm_103a")
 
 
+_MEASURED = []
+
+
+@pytest.fixture
+def measured(request):
+    """measured(name, value): records a value the test measured (an error
+    against the oracle, a mismatch count) for the end-of-run summary, which
+    pytest prints even with -q."""
+    def record(name, value):
+        _MEASURED.append((request.node.nodeid, name, value))
+    return record
+
+
+def pytest_terminal_summary(terminalreporter, exitstatus, config):
+    if _MEASURED:
+        terminalreporter.write_sep("-", "measured values")
+        for nodeid, name, value in _MEASURED:
+            terminalreporter.write_line(f"{nodeid}: {name} = {value}")
+
+
 @pytest.fixture(scope="session")
 def oracle():
     from oracle import oracle as orc

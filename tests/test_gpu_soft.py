@@ -42,7 +42,7 @@ def sphere_renderer(device="cuda"):
     return r
 
 
-def test_soft_forward_matches_oracle(cuda):
+def test_soft_forward_matches_oracle(cuda, measured):
     for r in (soft_cartpole(8), sphere_renderer()):
         if hasattr(r, "cart"):
             r._step(workloads.cartpole_states(8, seed=33, device=cuda))
@@ -51,6 +51,7 @@ def test_soft_forward_matches_oracle(cuda):
         ref = oracle.render_soft(sc, me, no, out_dtype=np.float64)
         err = np.abs(img - ref).max()
         print("soft forward max |gpu - fp64|:", err)
+        measured("max |gpu - fp64| (" + ("cartpole" if hasattr(r, "cart") else "spheres") + ")", f"{err:.2e}")
         assert err <= 2e-4
         assert ref.max() > 0.05
 
@@ -88,7 +89,7 @@ def _dense_reference_errors(r, target):
     return errs
 
 
-def test_soft_gradients_match_dense_torch_reference(cuda):
+def test_soft_gradients_match_dense_torch_reference(cuda, measured):
     """Adjoint kernel against autograd through the dense float64 PyTorch
     restatement.  The kernels compute in float32, and with the softmax
     temperature 1e-3 the gradient is sensitive to float32 rounding of the
@@ -103,16 +104,18 @@ def test_soft_gradients_match_dense_torch_reference(cuda):
     target = torch.rand((4, 3, 48, 48), generator=torch.Generator().manual_seed(40)).to(cuda) * 0.3
     errs = _dense_reference_errors(r, target)
     print("cartpole: gpu vs dense fp64 torch gradient relative errors:", errs)
+    measured("cartpole gradient relative errors", {k: f"{v:.2e}" for k, v in errs.items()})
     assert max(errs.values()) <= 1.5e-4, errs
     r = sphere_renderer()
     target = torch.rand((3, 3, 32, 40), generator=torch.Generator().manual_seed(34)).to(cuda) * 0.3
     errs = _dense_reference_errors(r, target)
     print("spheres: gpu vs dense fp64 torch gradient relative errors:", errs)
+    measured("spheres gradient relative errors", {k: f"{v:.2e}" for k, v in errs.items()})
     assert max(errs.values()) <= 2e-3, errs
 
 
 @pytest.mark.parametrize("sigma", [None, 0.5], ids=["edge10to90_0.5px", "sigma_0.5px"])
-def test_soft_cartpole_fd_check(cuda, sigma):
+def test_soft_cartpole_fd_check(cuda, sigma, measured):
     """Differentiable CartPole: 8 scenes at 64x64, loss = MSE against targets
     rendered at states perturbed by N(0, 0.05); gradients w.r.t. per-instance
     position, HPR and colour and the light direction, against FP64 central
@@ -151,6 +154,7 @@ def test_soft_cartpole_fd_check(cuda, sigma):
     err = rel_err(got, want)
     msg = f"soft CartPole FD check (sigma {sc['sigma']:.4f} px): {len(got)} parameters, relative error {err:.3e}"
     print(msg)
+    measured("FD relative error over 147 parameters", f"{err:.3e}")
     assert len(got) == 147, msg
     assert err <= (1e-5 if sigma is None else 1e-4), msg
 
@@ -178,7 +182,7 @@ def test_soft_step_and_optimisation(cuda):
 
 
 @pytest.mark.parametrize("n", [6, 2600])
-def test_soft_warp_and_tile_kernels_agree(cuda, n):
+def test_soft_warp_and_tile_kernels_agree(cuda, n, measured):
     """The scene-per-warp soft kernels (forward and adjoint) against the tile
     kernels on the same CartPole scenes: same model, different work layout
     and summation order.  6 scenes run several warps per scene, 2600 scenes
@@ -196,12 +200,13 @@ def test_soft_warp_and_tile_kernels_agree(cuda, n):
     d_img = (res["warp"][0] - res["tile"][0]).abs().max().item()
     g_err = rel_err(res["warp"][1].numpy(), res["tile"][1].numpy())
     print(f"soft warp vs tile: image {d_img:.2e}, gradient {g_err:.2e}")
+    measured("warp vs tile: image, gradient", f"{d_img:.2e}, {g_err:.2e}")
     assert d_img <= 1e-6
     assert g_err <= 1e-5
 
 
 @pytest.mark.parametrize("scene", ["spheres", "large"])
-def test_soft_binned_and_tile_kernels_agree(cuda, scene):
+def test_soft_binned_and_tile_kernels_agree(cuda, scene, measured):
     """The binned soft kernels (default for scenes over 128 triangles) against
     the tile kernels: the sphere scene, and 6 scenes of the large soft
     configuration's kind (64 icosphere-s2 + 64 cubes per scene, 96x96).
@@ -228,5 +233,6 @@ def test_soft_binned_and_tile_kernels_agree(cuda, scene):
     d_img = (res["binned"][0] - res["tile"][0]).abs().max().item()
     g_err = rel_err(res["binned"][1].numpy(), res["tile"][1].numpy())
     print(f"soft binned vs tile ({scene}): image {d_img:.2e}, gradient {g_err:.2e}")
+    measured("binned vs tile: image, gradient", f"{d_img:.2e}, {g_err:.2e}")
     assert d_img <= 1e-6
     assert g_err <= 2e-4

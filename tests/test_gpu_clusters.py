@@ -129,3 +129,19 @@ def test_pretest_leaves_pixels_unchanged(cuda, scenes):
         res.append(_render_all(r))
     _assert_same(*res)
     assert (res[0][2] >= 0).float().mean() > 0.05
+
+
+def test_pretest_leaves_plain_per_node_draws_unchanged(cuda):
+    """The per-node plain path (one tile-kernel draw per node against the depth
+    and colour buffers of the nodes drawn before, whose keys carry order 0):
+    the pre-test forced on and off gives bit-identical pixels and depth on
+    dense uneven scenes."""
+    res = []
+    for mode in ("on", "off"):
+        r = workloads.uneven(num_scenes=48, res=84, max_instances=256, seed=13, raster_kernel="tile",
+                             raster_method="plain", tile_pretest=mode)
+        out, depth = r.render(return_depth=True)
+        torch.cuda.synchronize()
+        res.append((out.clone(), depth.clone()))
+    _assert_same(*res)
+    assert (res[0][1] < 1.0).float().mean() > 0.05

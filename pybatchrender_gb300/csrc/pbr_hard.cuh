@@ -185,8 +185,11 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
   uint32_t* s_keep = reinterpret_cast<uint32_t*>(s_item + 4);           // [kInstWords] kept instances of a batch
   int* s_ci = reinterpret_cast<int*>(s_keep + kInstWords);              // [kMaxInstBatch] their batch indices
   int* s_pairs = reinterpret_cast<int*>(smem + L.pairs);  // [kMaxClusterPairs] kept (instance, cluster) pairs
+  int2* s_wq = reinterpret_cast<int2*>(smem + L.wq);      // [NW][kWarpQueue] kept triangles waiting to be written
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int2* const wq = s_wq + warp * kWarpQueue;
+  int qn = 0;  // this warp's queued kept triangles (the same in every lane)
   const int W = P.W, H = P.H;
   const int HW = W * H;
   const int words = A.tri_cap >> 5;
@@ -575,6 +578,86 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
         // list; each pair is tested (cluster_culled) and the survivors compacted in draw order, then the
         // triangle rounds run over the kept pairs' triangles only.  The culled clusters hold no triangle that
         // would be drawn, so the output is the same as without clusters.
+        // clip coordinates of source triangle (i0, i1, i2) of batch instance li
+        auto clip3 = [&](int li, int i0, int i1, int i2, float4 cv[3]) {
+          if (use_mvp) {
+            const float4 m0 = icache[li * IS + 4], m1 = icache[li * IS + 5], m2 = icache[li * IS + 6];
+            const float4 m3 = icache[li * IS + 7];
+            const int iv[3] = {i0, i1, i2};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const int vi = (int)PBR_IX(iv[q], me.nv, 5);
+              const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
+              cv[q] = make_float4(fmaf(m0.x, ox, fmaf(m0.y, oy, fmaf(m0.z, oz, m0.w))),
+                                  fmaf(m1.x, ox, fmaf(m1.y, oy, fmaf(m1.z, oz, m1.w))),
+                                  fmaf(m2.x, ox, fmaf(m2.y, oy, fmaf(m2.z, oz, m2.w))),
+                                  fmaf(m3.x, ox, fmaf(m3.y, oy, fmaf(m3.z, oz, m3.w))));
+            }
+          } else {
+            const float4 r0 = icache[li * IS + 0], r1 = icache[li * IS + 1], r2 = icache[li * IS + 2];
+            cv[0] = clip_of(me, i0, r0, r1, r2);
+            cv[1] = clip_of(me, i1, r0, r1, r2);
+            cv[2] = clip_of(me, i2, r0, r1, r2);
+          }
+        };
+        // Kept triangles wait in their warp's queue -- (source triangle; instance, slot count, front, slot) -- and
+        // are set up 32 at a time, one per lane, when the queue holds 32, before a chunk flush and at the end of
+        // the instance batch: a round's few survivors no longer hold most warps in the long write path.  The
+        // writer repeats the vertex transform (the same arithmetic, so the same screen coordinates) and fills
+        // exactly the slots the count reserved (an empty record where it does not emit the triangle).
+        auto write_queued = [&](int2 e) {
+          const int ti = (int)PBR_IX(e.x, nt, 4), li = (int)PBR_IX(e.y & 0xff, A.icap, 1);
+          const int c = (e.y >> 8) & 3, slot = e.y >> 11;
+          const bool front = ((e.y >> 10) & 1) != 0;
+          const int i0 = me.idx[3 * ti], i1 = me.idx[3 * ti + 1], i2 = me.idx[3 * ti + 2];
+          float4 cv[3];
+          clip3(li, i0, i1, i2, cv);
+          const float4 r0 = icache[li * IS + 0], r1 = icache[li * IS + 1], r2 = icache[li * IS + 2];
+          const float4 col = icache[li * IS + 3];
+          const int draw_id = (nd.rank_base + b0 + li) * P.max_tris + ti;
+          // world normals: the provoking vertex's for flat meshes (the three are identical), all three if smooth
+          float4 nv[3];
+          const int iv[3] = {i0, i1, i2};
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            if (q == 0 || smooth) {
+              const int vi = (int)PBR_IX(iv[q], me.nv, 6);
+              const float ax = me.nrm[3 * vi], ay = me.nrm[3 * vi + 1], az = me.nrm[3 * vi + 2];
+              const float nx = r0.x * ax + r0.y * ay + r0.z * az;
+              const float ny = r1.x * ax + r1.y * ay + r1.z * az;
+              const float nz = r2.x * ax + r2.y * ay + r2.z * az;
+              const float l2 = nx * nx + ny * ny + nz * nz;
+              const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
+              nv[q] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
+            } else {
+              nv[q] = nv[0];
+            }
+          }
+          TexIn tx;
+          if (textured) {
+            tx.t0 = mesh_uv(me, i0);
+            tx.t1 = mesh_uv(me, i1);
+            tx.t2 = mesh_uv(me, i2);
+            tx.node = n;
+          }
+          if (front) {
+            SV sv[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) sv[q] = to_screen(cv[q], S.W, S.H);
+            if (!setup_tri_sv<true>(P, S, sv[0], nv[0], sv[1], nv[1], sv[2], nv[2], slot, col, draw_id, smooth, tx))
+              write_empty(S, slot);
+          } else {
+            clip_tri<true>(P, S, cv[0], nv[0], cv[1], nv[1], cv[2], nv[2], i0, i1, i2, slot, col, draw_id, smooth, tx,
+                           c);
+          }
+        };
+        // the warp's last m queued triangles, one per lane (warp-uniform m <= 32)
+        auto drain = [&](int m) {
+          __syncwarp();
+          if (lane < m) write_queued(wq[qn - m + lane]);
+          __syncwarp();
+          qn -= m;
+        };
         const bool use_cl = A.cl_any && me.clusters != nullptr && me.ncl > 0;
         const int per_sub = use_cl ? max(1, kMaxClusterPairs / me.ncl) : max(nb, 1);
         for (int s0 = 0; s0 < nb; s0 += per_sub) {
@@ -643,25 +726,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             i0 = me.idx[3 * ti];
             i1 = me.idx[3 * ti + 1];
             i2 = me.idx[3 * ti + 2];
-            if (use_mvp) {
-              const float4 m0 = icache[li * IS + 4], m1 = icache[li * IS + 5], m2 = icache[li * IS + 6];
-              const float4 m3 = icache[li * IS + 7];
-              const int iv[3] = {i0, i1, i2};
-#pragma unroll
-              for (int q = 0; q < 3; ++q) {
-                const int vi = (int)PBR_IX(iv[q], me.nv, 5);
-                const float ox = me.pos[3 * vi], oy = me.pos[3 * vi + 1], oz = me.pos[3 * vi + 2];
-                cv[q] = make_float4(fmaf(m0.x, ox, fmaf(m0.y, oy, fmaf(m0.z, oz, m0.w))),
-                                    fmaf(m1.x, ox, fmaf(m1.y, oy, fmaf(m1.z, oz, m1.w))),
-                                    fmaf(m2.x, ox, fmaf(m2.y, oy, fmaf(m2.z, oz, m2.w))),
-                                    fmaf(m3.x, ox, fmaf(m3.y, oy, fmaf(m3.z, oz, m3.w))));
-              }
-            } else {
-              const float4 r0 = icache[li * IS + 0], r1 = icache[li * IS + 1], r2 = icache[li * IS + 2];
-              cv[0] = clip_of(me, i0, r0, r1, r2);
-              cv[1] = clip_of(me, i1, r0, r1, r2);
-              cv[2] = clip_of(me, i2, r0, r1, r2);
-            }
+            clip3(li, i0, i1, i2, cv);
             const float d0 = cv[0].z + cv[0].w, d1 = cv[1].z + cv[1].w, d2 = cv[2].z + cv[2].w;
             front = d0 >= 0.f && d1 >= 0.f && d2 >= 0.f;
             const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -672,19 +737,6 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
                              : setup_tri_sv<false>(P, S, sv[0], z4, sv[1], z4, sv[2], z4, 0, z4, 0, smooth);
             } else if (!(d0 < 0.f && d1 < 0.f && d2 < 0.f)) {
               c = clip_tri<false>(P, S, cv[0], z4, cv[1], z4, cv[2], z4, i0, i1, i2, 0, z4, 0, smooth);
-            }
-          }
-          // a kept smooth triangle's three vertex normals are loaded now, so that their latency overlaps the
-          // compaction below (a flat triangle loads its one normal in the write pass)
-          float an[9];
-          if (c > 0 && smooth) {
-            const int iv[3] = {i0, i1, i2};
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              const int vi = (int)PBR_IX(iv[q], me.nv, 6);
-              an[3 * q] = me.nrm[3 * vi];
-              an[3 * q + 1] = me.nrm[3 * vi + 1];
-              an[3 * q + 2] = me.nrm[3 * vi + 2];
             }
           }
           // draw-order compaction: warp prefix sum, then the totals of the warps before this one
@@ -706,62 +758,24 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           }
           parity ^= 1;
           // A round emits at most 2 triangles per source triangle (near-plane clip), so total <= 2 * RT <= tri_cap:
-          // the chunk is flushed only when this round's kept triangles do not fit; they keep their setup inputs in
-          // registers across the flush.
-          if (tri_count + total > A.tri_cap) flush(false);
+          // the chunk is flushed (its queued triangles written first) only when this round's kept triangles do not
+          // fit
+          if (tri_count + total > A.tri_cap) {
+            if (qn > 0) drain(qn);
+            flush(false);
+          }
+          const uint32_t kept = __ballot_sync(0xffffffffu, c > 0);
           if (c > 0) {
             const int slot0 = tri_count + before + incl - c, last = slot0 + c - 1;
             const int slot = (int)PBR_IX(last, A.tri_cap, 8) == last ? slot0 : 0;
-            const float4 r0 = icache[li * IS + 0], r1 = icache[li * IS + 1], r2 = icache[li * IS + 2];
-            const float4 col = icache[li * IS + 3];
-            const int draw_id = (nd.rank_base + b0 + li) * P.max_tris + ti;
-            // world normals: the provoking vertex's for flat meshes (the three are identical), all three if smooth
-            float4 nv[3];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              if (q == 0 || smooth) {
-                float ax, ay, az;
-                if (smooth) {
-                  ax = an[3 * q];
-                  ay = an[3 * q + 1];
-                  az = an[3 * q + 2];
-                } else {
-                  const int vi = (int)PBR_IX(i0, me.nv, 6);
-                  ax = me.nrm[3 * vi];
-                  ay = me.nrm[3 * vi + 1];
-                  az = me.nrm[3 * vi + 2];
-                }
-                const float nx = r0.x * ax + r0.y * ay + r0.z * az;
-                const float ny = r1.x * ax + r1.y * ay + r1.z * az;
-                const float nz = r2.x * ax + r2.y * ay + r2.z * az;
-                const float l2 = nx * nx + ny * ny + nz * nz;
-                const float inv = l2 > 0.f ? rsqrtf(l2) : 0.f;
-                nv[q] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
-              } else {
-                nv[q] = nv[0];
-              }
-            }
-            TexIn tx;
-            if (textured) {
-              tx.t0 = mesh_uv(me, i0);
-              tx.t1 = mesh_uv(me, i1);
-              tx.t2 = mesh_uv(me, i2);
-              tx.node = n;
-            }
-            // Exactly the c slots this thread reserved are written, whatever the write pass decides: a triangle it
-            // rejects after all (the count pass and this pass are separate inlined copies of the setup) leaves an
-            // empty record, never the stale record of an earlier chunk or work item for the binner to read.
-            if (front) {
-              if (!setup_tri_sv<true>(P, S, sv[0], nv[0], sv[1], nv[1], sv[2], nv[2], slot, col, draw_id, smooth, tx))
-                write_empty(S, slot);
-            } else {
-              clip_tri<true>(P, S, cv[0], nv[0], cv[1], nv[1], cv[2], nv[2], i0, i1, i2, slot, col, draw_id, smooth, tx,
-                             c);
-            }
+            wq[qn + __popc(kept & ((1u << lane) - 1u))] = make_int2(ti, li | (c << 8) | (front ? 1 << 10 : 0) | (slot << 11));
           }
+          qn += __popc(kept);
+          if (qn >= 32) drain(32);
           tri_count += total;
         }
         }  // sub-batches
+        if (qn > 0) drain(qn);  // before the next batch replaces the instance matrices
       }
     }
     flush(true);

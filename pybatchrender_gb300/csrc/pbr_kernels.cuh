@@ -28,6 +28,7 @@ enum : int {
 
 constexpr int kClusterTris = 32;    // triangles per cluster (the last cluster of a mesh may hold fewer)
 constexpr int kMaxClusterPairs = 2048;
+constexpr int kWarpQueue = 64;    // tile kernel: a warp's queue of kept triangles (drained at 32, one round adds <= 32)
 constexpr int kMvpMinTris = 128;  // tile kernel: meshes this large transform vertices with a per-instance VP * M  // (instance, cluster) pairs the tile kernel compacts at a time
 
 struct MeshDesc {
@@ -135,6 +136,7 @@ struct SmemLayout {
   int state;               // per-pixel depth / emit-order keys of the region [threads*kPx] (uint64)
   int misc;                // per-warp survivor counts (two rounds), VP, work item, instance compaction
   int pairs;               // kept (instance, cluster) pairs [kMaxClusterPairs] and the scene's eye (float4)
+  int wq;                  // per-warp queues of kept triangles waiting to be written [threads/32][kWarpQueue] (int2)
   int total;
 };
 
@@ -170,6 +172,7 @@ __host__ __device__ inline SmemLayout smem_layout(const RasterArgs& a, int threa
   off += align16(threads * kPx * 8);
   L.misc = off; off += align16((2 * (threads / 32) + 8) * 4 + 16 * 4 + 16 + (kInstWords + kMaxInstBatch) * 4);
   L.pairs = off; off += a.cl_any ? align16(kMaxClusterPairs * 4 + 16) : 0;  // kept pairs; eye position
+  L.wq = off; off += align16((threads / 32) * kWarpQueue * 8);
   L.total = off;
   return L;
 }

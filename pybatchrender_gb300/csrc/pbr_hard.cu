@@ -7,18 +7,24 @@
 //
 //   K1  instance stage: per instance M = [R(hpr)*s | t]
 //       (renderer/shader_context.py:47-84, renderer/node.py:116-126), in
-//       batches of up to icap instances
+//       batches of up to icap instances; instances whose bounding sphere
+//       projects outside the region are dropped, and for meshes with clusters
+//       (groups of 32 triangles, pbr_mesh_set_clusters) so are the (instance,
+//       cluster) pairs that face away from the eye or hold no pixel centre
 //   K2  one source triangle per thread: its three vertices clip = VP[k] * M * v
-//       (shaders/basic.vert:29-53), near-plane clip, GL viewport transform into
-//       the scene's own image (basic.vert:45-52 + the atlas flip of
-//       renderer/frame_grabber.py:105), back-face cull, bbox; survivors get
-//       their world normal(s), watertight FP32 edge functions with the
-//       top-left rule, depth plane and flat shading, and are compacted in draw
-//       order (warp prefix sums + per-warp totals, one barrier per round) into
-//       a shared-memory triangle list ("chunk")
+//       (shaders/basic.vert:29-53; one per-instance VP * M for meshes of 128+
+//       triangles), near-plane clip, GL viewport transform into the scene's own
+//       image (basic.vert:45-52 + the atlas flip of
+//       renderer/frame_grabber.py:105), back-face cull, bbox, and in dense
+//       scenes an exact coverage-and-depth test against the pixels' current
+//       keys; the kept triangles are counted in draw order (warp prefix sums +
+//       per-warp totals, one barrier per round), which fixes their slots in a
+//       shared-memory triangle list ("chunk"), wait in their warp's queue and
+//       are set up 32 at a time: world normal(s), watertight FP32 edge
+//       functions with the top-left rule, depth plane and flat shading
 //       + warp-ballot binner: one __ballot_sync per (32 triangles, bin) builds
 //       the per-bin triangle bit masks
-//   K3  raster of the chunk, bin by bin (warps take bins in turn): the
+//   K3  raster of the chunk, (bin, mask word) items spread over the warps: the
 //       candidates' (triangle, pixel) pairs inside the bin are packed 32 per
 //       pass (prefix sum of the clipped bbox areas), so tiny triangles cost a
 //       few instructions each; every covered pixel does a 64-bit atomicMin of

@@ -768,7 +768,8 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           if (c > 0) {
             const int slot0 = tri_count + before + incl - c, last = slot0 + c - 1;
             const int slot = (int)PBR_IX(last, A.tri_cap, 8) == last ? slot0 : 0;
-            wq[qn + __popc(kept & ((1u << lane) - 1u))] = make_int2(ti, li | (c << 8) | (front ? 1 << 10 : 0) | (slot << 11));
+            const int packed = li | (c << 8) | (front ? 1 << 10 : 0) | (slot << 11);
+            wq[qn + __popc(kept & ((1u << lane) - 1u))] = make_int2(ti, packed);
           }
           qn += __popc(kept);
           if (qn >= 32) drain(32);

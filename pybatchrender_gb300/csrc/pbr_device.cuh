@@ -6,8 +6,30 @@
 #pragma once
 
 #include "pbr_kernels.cuh"
+#ifdef PBR_SELFCHECK
+#include <cstdio>
+#endif
 
 namespace pbr {
+
+// Self-checks, compiled in with -DPBR_SELFCHECK only (a debugging build): every
+// index wrapped in PBR_IX is checked against the length of the buffer it addresses; a bad
+// one is printed (the first 32 per process) and replaced by 0, so that the
+// access stays inside the buffer.  Without the macro PBR_IX is the index.
+#ifdef PBR_SELFCHECK
+static __device__ int g_selfcheck_reports;
+static __device__ __noinline__ long long selfcheck_index(long long i, long long n, int site) {
+  if (i >= 0 && i < n) return i;
+  if (atomicAdd(&g_selfcheck_reports, 1) < 32)
+    printf("pbr selfcheck: site %d block %d thread %d index %lld of %lld\n", site, (int)blockIdx.x,
+           (int)threadIdx.x, i, n);
+  return 0;
+}
+#define PBR_IX(i, n, site) selfcheck_index((long long)(i), (long long)(n), (site))
+#else
+#define PBR_IX(i, n, site) (i)
+#endif
+
 
 __device__ __forceinline__ float clamp01f(float v) { return fminf(fmaxf(v, 0.f), 1.f); }
 

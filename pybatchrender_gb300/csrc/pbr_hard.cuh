@@ -4,29 +4,8 @@
 #pragma once
 
 #include "pbr_device.cuh"
-#ifdef PBR_SELFCHECK
-#include <cstdio>
-#endif
 
 namespace pbr {
-
-// Self-checks, compiled in with -DPBR_SELFCHECK only (a debugging build): every
-// index below is checked against the length of the buffer it addresses; a bad
-// one is printed (the first 32 per process) and replaced by 0, so that the
-// access stays inside the buffer.  Without the macro PBR_IX is the index.
-#ifdef PBR_SELFCHECK
-static __device__ int g_selfcheck_reports;
-static __device__ __noinline__ long long selfcheck_index(long long i, long long n, int site) {
-  if (i >= 0 && i < n) return i;
-  if (atomicAdd(&g_selfcheck_reports, 1) < 32)
-    printf("pbr selfcheck: site %d block %d thread %d index %lld of %lld\n", site, (int)blockIdx.x,
-           (int)threadIdx.x, i, n);
-  return 0;
-}
-#define PBR_IX(i, n, site) selfcheck_index((long long)(i), (long long)(n), (site))
-#else
-#define PBR_IX(i, n, site) (i)
-#endif
 
 // Whether no triangle of a cluster (bounding sphere cs, normal cone ca) of an
 // instance (model matrix rows r0..r2) can be drawn in the rows [ry0, ry1] of

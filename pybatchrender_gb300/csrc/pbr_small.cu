@@ -131,9 +131,10 @@ __device__ __forceinline__ int small_tri(const SceneParams& P, const SetupCtx& S
   while (inst + 1 < total_inst && __float_as_int(itab[(inst + 1) * 5 + 4].w) <= t) ++inst;
   const float4 meta = itab[inst * 5 + 4];
   const MeshDesc& me = P.meshes[P.nodes[__float_as_int(meta.x)].mesh];
-  const int ti = t - __float_as_int(meta.w);
+  const int ti = (int)PBR_IX(t - __float_as_int(meta.w), me.nt, 20);
   const int vbase = __float_as_int(meta.y);
-  const int i0 = me.idx[3 * ti], i1 = me.idx[3 * ti + 1], i2 = me.idx[3 * ti + 2];
+  const int i0 = (int)PBR_IX(me.idx[3 * ti], me.nv, 21), i1 = (int)PBR_IX(me.idx[3 * ti + 1], me.nv, 21);
+  const int i2 = (int)PBR_IX(me.idx[3 * ti + 2], me.nv, 21);
   float4 n0 = vcache[3 * (vbase + i0) + 1], n1 = vcache[3 * (vbase + i1) + 1], n2 = vcache[3 * (vbase + i2) + 1];
   const bool front = n0.w >= 0.f && n1.w >= 0.f && n2.w >= 0.f;
   if (!front && n0.w < 0.f && n1.w < 0.f && n2.w < 0.f) return 0;
@@ -323,6 +324,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
           nv.z = nz * inv;
         }
         const SV sv = to_screen(c, S.W, S.H);
+        (void)PBR_IX(v, A.vcap, 23);
         vcache[3 * v] = c;
         vcache[3 * v + 1] = nv;
         vcache[3 * v + 2] = make_float4(sv.x, sv.y, sv.z, sv.iw);
@@ -336,6 +338,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
     // holds no triangle gets an empty row range (first row 0xffff, last row
     // 0), which puts it in no bin.  Slot order is draw order.
     for (int t = lane; t < total_tris; t += 32) {
+      (void)PBR_IX(2 * t + 1, A.tri_cap, 22);
       const int c = small_tri<true, SMOOTH, TEX>(P, S, vcache, itab, total_inst, t, 2 * t);
       const float no_rows = __uint_as_float(0xffffu);
       if (c < 1) reinterpret_cast<float*>(&S.T4[2 * t])[0] = no_rows;
@@ -362,7 +365,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
         const bool yin = (by >= by0) && (by <= by1);
         for (int bx = 0; bx < bins_x; ++bx, ++b) {
           const uint32_t m = __ballot_sync(0xffffffffu, yin && (bx >= bx0) && (bx <= bx1));
-          if (lane == 0) masks[b * words + w] = m;
+          if (lane == 0) masks[PBR_IX(b * words + w, nbins * words, 24)] = m;
           ne |= (unsigned long long)(m != 0u) << b;
         }
       }
@@ -422,7 +425,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
         }
         __syncwarp();
         for (int w = 0; w < nw; ++w) {
-          const uint32_t m = masks[b * words + w];
+          const uint32_t m = masks[PBR_IX(b * words + w, nbins * words, 24)];
           if (m == 0u) continue;
           // this lane's candidate (triangle w*32+lane if its bit is set) and its bbox-in-bin
           int ax0 = 0, ay0 = 0, bw = 1, npx = 0;
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
             const int o_bw = __shfl_sync(0xffffffffu, bw, o);
             const float o_ibw = __shfl_sync(0xffffffffu, ibw, o);
             if (g >= total) continue;
-            const int t = w * 32 + o;
+            const int t = (int)PBR_IX(w * 32 + o, A.tri_cap, 25);
             const int local = g - o_start;
             // row within the bbox: (local + 0.5) / bw lies at least 0.5 / bw >= 1/64 from an
             // integer, far more than the error of the approximate reciprocal product
@@ -482,7 +485,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
               // z >= 0, so its bits order like the values (the mask folds -0 into +0)
               const unsigned long long key =
                   ((unsigned long long)(__float_as_uint(z) & 0x7fffffffu) << 32) | (unsigned)(t + 1);
-              atomicMin(&keys[(p & 15) * 32 + (p >> 4)], key);
+              atomicMin(&keys[PBR_IX((p & 15) * 32 + (p >> 4), kBinPx, 26)], key);
             }
           }
         }
@@ -497,7 +500,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, kMinBlocks) small_kernel(const
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
               const int j = 4 * g + q;
-              const uint32_t r = klo[64 * j];
+              const uint32_t r = (uint32_t)PBR_IX(klo[64 * j], A.tri_cap + 1, 27);
               const float4* rec = reinterpret_cast<const float4*>(rec4 + 16 * r);
               if (PLAIN && r == 0) {
                 col[q] = A.cbuf[lane_pix + boff + j];

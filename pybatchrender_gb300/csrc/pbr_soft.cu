@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
       if (BACKWARD) {
         // per triangle: chain to clip -> world -> model matrix, per instance
         for (int t = tid; t < T; t += THREADS) {
-          soft_tri_chain(P, S, t, tacc + t * 24, s_vp, iacc, s_light);
+          soft_tri_chain(P, S, t, tacc + t * 24, s_vp, iacc, A.iacc_cap, s_light);
         }
         __syncthreads();
       }

@@ -380,8 +380,8 @@ __device__ __forceinline__ void soft_grad(const SceneParams& P, const Frag& f, S
 // per-instance accumulators iacc[slot][kIacc] and the light gradient
 // light[3] (shared-memory atomics).
 __device__ __forceinline__ void soft_tri_chain(const SceneParams& P, const SoftCtx& S, int t, const float* ta,
-                                               const float* s_vp, float* iacc, float* s_light) {
-  const int slot = __float_as_int(S.R[5][t].z);
+                                               const float* s_vp, float* iacc, int iacc_cap, float* s_light) {
+  const int slot = (int)PBR_IX(__float_as_int(S.R[5][t].z), iacc_cap, 35);
   float* ia = iacc + slot * kIacc;
   // instance slot -> node
   int n = 0;

@@ -147,8 +147,8 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
           float4 cv[3], nv[3];
           if (t0 + tid < total_t) {
             const int t = t0 + tid;
-            li = t / nt;
-            const int ti = t - li * nt;
+            li = (int)PBR_IX(t / nt, A.icap, 34);
+            const int ti = t - (t / nt) * nt;
             iv[0] = me.idx[3 * ti];
             iv[1] = me.idx[3 * ti + 1];
             iv[2] = me.idx[3 * ti + 2];
@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
           }
           parity ^= 1;
           if (c > 0) {
-            const int slot = T + before + incl - c;
+            const int slot = (int)PBR_IX(T + before + incl - c, cap, 30);
             const float4 r0 = icache[li * 4 + 0], r1 = icache[li * 4 + 1], r2 = icache[li * 4 + 2];
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
@@ -220,7 +220,8 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
             if (px0 <= px1 && py0 <= py1)
               for (int by = by0; by <= by1; ++by)
                 for (int bx = bx0; bx <= bx1; ++bx)
-                  atomicOr(&bmask[(long long)(by * nbx + bx) * words + (slot >> 5)], bit);
+                  atomicOr(&bmask[PBR_IX((long long)(by * nbx + bx) * words + (slot >> 5), (long long)nblocks * words, 31)],
+                           bit);
           }
           T += total;
         }
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
             nzw &= nzw - 1u;
             uint32_t mk = __shfl_sync(0xffffffffu, mine, j);
             while (mk) {
-              const int t = (w0 + j) * 32 + __ffs(mk) - 1;
+              const int t = (int)PBR_IX((w0 + j) * 32 + __ffs(mk) - 1, cap, 32);
               mk &= mk - 1u;
               if (mk) prefetch_record(slab, cap, (w0 + j) * 32 + __ffs(mk) - 1, lane);
               Frag f;
@@ -345,7 +346,7 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
             nzw &= nzw - 1u;
             uint32_t mk = __shfl_sync(0xffffffffu, mine, j);
             while (mk) {
-              const int t = (w0 + j) * 32 + __ffs(mk) - 1;
+              const int t = (int)PBR_IX((w0 + j) * 32 + __ffs(mk) - 1, cap, 32);
               mk &= mk - 1u;
               if (mk) prefetch_record(slab, cap, (w0 + j) * 32 + __ffs(mk) - 1, lane);
               float acc[24];
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
               if (__any_sync(0xffffffffu, hit)) {
                 int idx;
                 const float v = warp_reduce24(acc, lane, idx);
-                if ((lane & 3) != 3 && v != 0.f) atomicAdd(&tacc[(long long)t * 24 + idx], v);
+                if ((lane & 3) != 3 && v != 0.f) atomicAdd(&tacc[PBR_IX((long long)t * 24 + idx, (long long)cap * 24, 33)], v);
               }
             }
           }
@@ -376,7 +377,8 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
     if (BACKWARD) {
       __syncthreads();
       // ---- C: survivor -> instance -> pose, scale, colour ------------------------
-      for (int t = tid; t < T; t += kLargeThreads) soft_tri_chain(P, S, t, tacc + (long long)t * 24, s_vp, iacc, s_light);
+      for (int t = tid; t < T; t += kLargeThreads)
+        soft_tri_chain(P, S, t, tacc + (long long)t * 24, s_vp, iacc, A.iacc_cap, s_light);
       __syncthreads();
       for (int s = tid; s < A.iacc_cap; s += kLargeThreads) soft_instance_grads(P, k, s, iacc + s * kIacc);
       if (tid < 3 && A.glight) atomicAdd(&A.glight[tid], s_light[tid]);

@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(kSoftWarps * 32) soft_small_kernel(const __gri
     if (BACKWARD) {
       __syncwarp();
       // ---- K4: triangle -> instance -> pose, scale, colour ------------------
-      for (int t = lane; t < T; t += 32) soft_tri_chain(P, S, t, tacc + t * 24, s_vp, iacc, s_light);
+      for (int t = lane; t < T; t += 32) soft_tri_chain(P, S, t, tacc + t * 24, s_vp, iacc, A.iacc_cap, s_light);
       __syncwarp();
       for (int s = lane; s < total_inst; s += 32) {
         // this scene's instance s is the instance slot stored in its meta

@@ -228,10 +228,12 @@ int pbr_soft_config(pbr_ctx* ctx, float sigma, float gamma, int threads);
  * NULL): d_gpos [B,3], d_ghpr [B,3], d_gscale [B], d_gcol [B,4] (alpha gets 0). */
 int pbr_node_set_grads(pbr_ctx* ctx, int node_id, float* d_gpos, float* d_ghpr, float* d_gscale, float* d_gcol);
 
-/* Soft forward: d_out [N,3,H,W] float32; d_stats [N,H,W,8] float32 (optional,
+/* Soft forward: d_out [N,3,H,W] float32; d_stats 6*N*H*W float32 (optional,
  * needed by the backward, 16-byte aligned): per pixel the largest normalised
  * depth m, the softmax denominator relative to it, a code for prod(1 - D),
- * and the blended colour relative to the first fragment's colour. */
+ * and the blended colour relative to the first fragment's colour (dl), stored
+ * as N*H*W float4 (m, denominator, code, dl[0]) followed by N*H*W float2
+ * (dl[1], dl[2]). */
 int pbr_render_soft(pbr_ctx* ctx, float* d_out, float* d_stats, void* stream);
 
 /* Soft adjoint: given the forward's d_out and d_stats and dL/dout

@@ -125,14 +125,15 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
         float Lv = -1e30f, Sv = 1.f, code = 1.f, Av = 0.f, cf[3] = {0.f, 0.f, 0.f}, g[3] = {0.f, 0.f, 0.f};
         float dl[3] = {0.f, 0.f, 0.f};
         if (active && q < p1) {
-          const float4 stv = *reinterpret_cast<const float4*>(A.stats + 8 * ((long long)k * HW + q));
-          const float4 stw = *reinterpret_cast<const float4*>(A.stats + 8 * ((long long)k * HW + q) + 4);
+          float4 stv;
+          float2 stw;
+          stats_load(A.stats, (long long)P.N * HW, (long long)k * HW + q, stv, stw);
           Lv = stv.x;
           Sv = stv.y;
           code = stv.z;
-          dl[0] = stw.x;
-          dl[1] = stw.y;
-          dl[2] = stw.z;
+          dl[0] = stv.w;
+          dl[1] = stw.x;
+          dl[2] = stw.y;
           float Pnz, nz;
           if (code >= 0.f) { Pnz = code; nz = 0.f; } else if (code >= -2.f) { Pnz = -1.f - code; nz = 1.f; } else { Pnz = 0.f; nz = 2.f; }
           Av = nz > 0.f ? 1.f : 1.f - Pnz;
@@ -438,9 +439,8 @@ __global__ void __launch_bounds__(THREADS) soft_kernel(const __grid_constant__ S
           if (A.stats) {
             // coverage code: prod over non-zero (1 - D), folded with the count of zero factors
             const float code = nz == 0.f ? Pv : (nz == 1.f ? -1.f - Pv : -3.f);
-            float4* so = reinterpret_cast<float4*>(A.stats + 8 * ((long long)k * HW + q));
-            so[0] = make_float4(m0, S0, code, 0.f);
-            so[1] = make_float4(dl[0], dl[1], dl[2], 0.f);
+            stats_store(A.stats, (long long)P.N * HW, (long long)k * HW + q, make_float4(m0, S0, code, dl[0]),
+                        make_float2(dl[1], dl[2]));
           }
         }
       }

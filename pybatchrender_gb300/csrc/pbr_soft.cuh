@@ -252,6 +252,21 @@ __device__ __forceinline__ bool soft_frag(const SceneParams& P, const SoftCtx& S
 // Per-pixel adjoint state: max zs, prod(1 - D) over non-unit factors and their
 // count, dL/dA, Cfg - C_r from the forward, dL/dCfg = A dL/dout, 1/S, and the
 // colour reference C_r of the first fragment (set on the first call).
+// The soft forward's per-pixel statistics for its adjoint, 24 bytes a pixel in
+// one [6 * npx] float32 buffer (npx = N * H * W): first a float4 per pixel (the
+// largest depth logit m, the softmax sum, the coverage code, dl[0]), then a
+// float2 per pixel (dl[1], dl[2]), where dl = (foreground colour) - (colour
+// reference); both accesses aligned.
+__device__ __forceinline__ void stats_store(float* stats, long long npx, long long q, float4 a, float2 b) {
+  reinterpret_cast<float4*>(stats)[q] = a;
+  reinterpret_cast<float2*>(stats + 4 * npx)[q] = b;
+}
+
+__device__ __forceinline__ void stats_load(const float* stats, long long npx, long long q, float4& a, float2& b) {
+  a = reinterpret_cast<const float4*>(stats)[q];
+  b = reinterpret_cast<const float2*>(stats + 4 * npx)[q];
+}
+
 struct SoftPixB {
   float m, Pnz, nz, dLdA, dl[3], dc[3], invS, Cr[3], ref;
 };

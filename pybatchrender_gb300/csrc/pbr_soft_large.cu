@@ -294,9 +294,7 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
           o[2 * HW] = Av * (cr2 + dl2) + (1.f - Av) * P.bg[2];
           if (A.stats) {
             const float code = nz == 0.f ? Pv : (nz == 1.f ? -1.f - Pv : -3.f);
-            float4* so = reinterpret_cast<float4*>(A.stats + 8 * q);
-            so[0] = make_float4(m, Ssum, code, 0.f);
-            so[1] = make_float4(dl0, dl1, dl2, 0.f);
+            stats_store(A.stats, (long long)P.N * HW, q, make_float4(m, Ssum, code, dl0), make_float2(dl1, dl2));
           }
         }
       } else {
@@ -314,8 +312,9 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
           pb.Cr[c] = 0.f;
         }
         if (active) {
-          const float4 stv = *reinterpret_cast<const float4*>(A.stats + 8 * q);
-          const float4 stw = *reinterpret_cast<const float4*>(A.stats + 8 * q + 4);
+          float4 stv;
+          float2 stw;
+          stats_load(A.stats, (long long)P.N * HW, q, stv, stw);
           const float code = stv.z;
           float Pnz, nzv;
           if (code >= 0.f) { Pnz = code; nzv = 0.f; } else if (code >= -2.f) { Pnz = -1.f - code; nzv = 1.f; } else { Pnz = 0.f; nzv = 2.f; }
@@ -332,9 +331,9 @@ __global__ void __launch_bounds__(kLargeThreads, 2) soft_large_kernel(const __gr
           pb.nz = nzv;
           pb.dLdA = g[0] * (cf[0] - P.bg[0]) + g[1] * (cf[1] - P.bg[1]) + g[2] * (cf[2] - P.bg[2]);
           pb.invS = stv.y > 0.f ? 1.f / stv.y : 0.f;
-          pb.dl[0] = stw.x;
-          pb.dl[1] = stw.y;
-          pb.dl[2] = stw.z;
+          pb.dl[0] = stv.w;
+          pb.dl[1] = stw.x;
+          pb.dl[2] = stw.y;
 #pragma unroll
           for (int c = 0; c < 3; ++c) pb.dc[c] = Av * g[c];
         }

@@ -335,7 +335,8 @@ class PBRRenderer:
             self._set_light_direction(light_dir)
         N, C, H, W = self._out_shape()
         out = torch.empty((N, 3, H, W), dtype=torch.float32, device=self.device)
-        stats = torch.empty((N, H, W, 8), dtype=torch.float32, device=self.device) if want_stats else None
+        # per pixel: float4 (m, softmax sum, coverage code, dl0) for all pixels, then float2 (dl1, dl2)
+        stats = torch.empty((6 * N * H * W,), dtype=torch.float32, device=self.device) if want_stats else None
         _capi.call(self._lib, self._ctx, "pbr_render_soft", _capi.ptr(out), _capi.ptr(stats), self._stream())
         return out, stats
 

@@ -173,7 +173,9 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
   const int HW = W * H;
   const int words = A.tri_cap >> 5;
   const int B = A.bin_px;
-  const int RT = min(THREADS, A.tri_cap >> 1);
+  // source triangles per round: every thread when a chunk holds THREADS records (a round that keeps more than
+  // a chunk is then placed in two halves of at most THREADS records each), else half a chunk
+  const int RT = A.tri_cap >= THREADS ? THREADS : (A.tri_cap >> 1);
   const int IS = A.mvp_any ? 8 : 4;  // float4 per cached instance: model rows, colour [, view-projection x model rows]
 
   for (int it = 0;; ++it) {
@@ -718,41 +720,60 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
               c = clip_tri<false>(P, S, cv[0], z4, cv[1], z4, cv[2], z4, i0, i1, i2, 0, z4, 0, smooth);
             }
           }
-          // draw-order compaction: warp prefix sum, then the totals of the warps before this one
-          int incl = c;
+          // draw-order compaction: warp prefix sum, then the totals of the warps before this one (one barrier)
+          auto compact = [&](int n, int& incl_o, int& before_o, int& total_o) {
+            int incl = n;
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-          }
-          int* wcnt = s_scan + parity * NW;
-          if (lane == 31) wcnt[warp] = incl;
-          __syncthreads();
-          int before = 0, total = 0;
+            for (int o = 1; o < 32; o <<= 1) {
+              const int y = __shfl_up_sync(0xffffffffu, incl, o);
+              if (lane >= o) incl += y;
+            }
+            int* wcnt = s_scan + parity * NW;
+            if (lane == 31) wcnt[warp] = incl;
+            __syncthreads();
+            int before = 0, total = 0;
 #pragma unroll
-          for (int w = 0; w < NW; ++w) {
-            const int v = wcnt[w];
-            before += w < warp ? v : 0;
-            total += v;
+            for (int w = 0; w < NW; ++w) {
+              const int v = wcnt[w];
+              before += w < warp ? v : 0;
+              total += v;
+            }
+            parity ^= 1;
+            incl_o = incl;
+            before_o = before;
+            total_o = total;
+          };
+          // the kept triangles' slots (the chunk flushed first, its queued triangles written, when they do not
+          // fit), then into the warp's queue
+          auto place = [&](int n, int incl, int before, int total) {
+            if (tri_count + total > A.tri_cap) {
+              if (qn > 0) drain(qn);
+              flush(false);
+            }
+            const uint32_t kept = __ballot_sync(0xffffffffu, n > 0);
+            if (n > 0) {
+              const int slot0 = tri_count + before + incl - n, last = slot0 + n - 1;
+              const int slot = (int)PBR_IX(last, A.tri_cap, 8) == last ? slot0 : 0;
+              const int packed = li | (n << 8) | (front ? 1 << 10 : 0) | (slot << 11);
+              wq[qn + __popc(kept & ((1u << lane) - 1u))] = make_int2(ti, packed);
+            }
+            qn += __popc(kept);
+            if (qn >= 32) drain(32);
+            tri_count += total;
+          };
+          int incl, before, total;
+          compact(c, incl, before, total);
+          if (total <= A.tri_cap) {
+            place(c, incl, before, total);
+          } else {
+            // more kept records than a chunk holds (many near-plane splits): the round's two halves in draw order,
+            // each at most THREADS records (RT = THREADS only when tri_cap >= THREADS)
+            for (int h = 0; h < 2; ++h) {
+              const int ch = ((tid < THREADS / 2) == (h == 0)) ? c : 0;
+              compact(ch, incl, before, total);
+              place(ch, incl, before, total);
+            }
           }
-          parity ^= 1;
-          // A round emits at most 2 triangles per source triangle (near-plane clip), so total <= 2 * RT <= tri_cap:
-          // the chunk is flushed (its queued triangles written first) only when this round's kept triangles do not
-          // fit
-          if (tri_count + total > A.tri_cap) {
-            if (qn > 0) drain(qn);
-            flush(false);
-          }
-          const uint32_t kept = __ballot_sync(0xffffffffu, c > 0);
-          if (c > 0) {
-            const int slot0 = tri_count + before + incl - c, last = slot0 + c - 1;
-            const int slot = (int)PBR_IX(last, A.tri_cap, 8) == last ? slot0 : 0;
-            const int packed = li | (c << 8) | (front ? 1 << 10 : 0) | (slot << 11);
-            wq[qn + __popc(kept & ((1u << lane) - 1u))] = make_int2(ti, packed);
-          }
-          qn += __popc(kept);
-          if (qn >= 32) drain(32);
-          tri_count += total;
         }
         }  // sub-batches
         if (qn > 0) drain(qn);  // before the next batch replaces the instance matrices

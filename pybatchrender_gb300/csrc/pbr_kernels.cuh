@@ -27,9 +27,9 @@ enum : int {
 };
 
 constexpr int kClusterTris = 32;    // triangles per cluster (the last cluster of a mesh may hold fewer)
-constexpr int kMaxClusterPairs = 2048;
-constexpr int kWarpQueue = 64;    // tile kernel: a warp's queue of kept triangles (drained at 32, one round adds <= 32)
-constexpr int kMvpMinTris = 128;  // tile kernel: meshes this large transform vertices with a per-instance VP * M  // (instance, cluster) pairs the tile kernel compacts at a time
+constexpr int kMaxClusterPairs = 2048;  // (instance, cluster) pairs the tile kernel compacts at a time
+constexpr int kWarpQueue = 64;    // tile kernel: a warp's queue of kept triangles (drained at 32, one placement adds <= 32)
+constexpr int kMvpMinTris = 128;  // tile kernel: meshes this large transform vertices with a per-instance VP * M
 
 struct MeshDesc {
   const float* pos;    // [nv,3]
@@ -107,7 +107,8 @@ struct RasterArgs {
 // Soft-coverage launch arguments (pbr_soft.cu).
 struct SoftArgs {
   float* out;          // forward: [N,3,H,W] output; backward: the forward's output (read)
-  float* stats;        // [N,H,W,8] (max zs, softmax denominator, coverage code, -, Cfg - C_r (3), -)
+  float* stats;        // [6*N*H*W]: float4 [N*H*W] (max zs, softmax denominator, coverage code, Cfg - C_r x),
+                       // then float2 [N*H*W] (Cfg - C_r y, z)
   const float* gout;   // backward: dL/dout [N,3,H,W]
   float* glight;       // backward: dL/d(normalised light direction) [3], accumulated
   int32_t* status;

@@ -190,6 +190,45 @@ def test_near_plane_clipping(cuda, oracle):
     cmp, gpu, ref = check_parity(r, oracle, depth_tol=1e-3)
 
 
+def test_round_keeps_more_records_than_a_chunk(cuda, oracle):
+    """Tile kernel, 256 threads, 256-triangle chunks: one source triangle per
+    thread and round, and every triangle of the fan crosses the near plane, so
+    a round keeps 2 records per triangle (512 > 256).  The round is then placed
+    in two halves of 128 triangles, in draw order.  Against the oracle and
+    against 512-triangle chunks (where the round fits whole)."""
+    from pybatchrender_gb300.renderer import meshes
+    # 320 copies of one triangle (two vertices in front of the eye, one behind it), each turned about the
+    # vertical axis through (0, 3, 0) and moved along the view axis, so that the copies cross one another
+    k = np.arange(320)
+    shift = ((k * 37) % 64) * 0.02
+    th = 0.15 * ((k * 13) % 7 - 3)
+    base = np.array([[-2.0, 0.0, -2.0], [2.0, 0.0, -2.0], [0.0, -6.0, 2.0]])
+    pos = np.empty((320, 3, 3), np.float32)
+    pos[:, :, 0] = np.cos(th)[:, None] * base[:, 0] - np.sin(th)[:, None] * base[:, 1]
+    pos[:, :, 1] = np.sin(th)[:, None] * base[:, 0] + np.cos(th)[:, None] * base[:, 1] + (3.0 + shift)[:, None]
+    pos[:, :, 2] = base[:, 2]
+    nrm = np.cross(pos[:, 1] - pos[:, 0], pos[:, 2] - pos[:, 0])
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    fan = meshes.Mesh(pos.reshape(-1, 3), np.repeat(nrm, 3, 0), np.arange(960).reshape(-1, 3), name="fan")
+    out = []
+    for cap in (256, 512):
+        r = pbr.PBRRenderer(num_scenes=2, tile_resolution=(64, 64), raster_kernel="tile", raster_threads=256,
+                            tri_cap=cap)
+        node = r.add_node(fan, 1)
+        node.set_colors(torch.tensor([[0.9, 0.5, 0.2, 1.0], [0.2, 0.7, 0.4, 1.0]]))
+        r.add_camera()
+        r._pbr_cam.set_positions_and_lookat(torch.tensor([[0.0, -0.4, 0.0], [0.1, -0.4, -0.1]]),
+                                            torch.tensor([[0.0, 5.0, 0.0], [0.0, 5.0, -0.3]]))
+        r.add_light()
+        r.setup_environment()
+        cmp, gpu, ref = check_parity(r, oracle, depth_tol=1e-3)
+        # the fan faces the eye and covers most of the image, with many copies winning somewhere
+        assert (ref["winner"] >= 0).mean() > 0.9 and len(np.unique(ref["winner"])) > 10, cmp
+        out.append(gpu)
+    for key in ("pixels", "winner", "depth"):
+        assert np.array_equal(out[0][key], out[1][key])
+
+
 def test_empty_and_degenerate_inputs(cuda, oracle):
     # no nodes at all: background everywhere
     r = pbr.PBRRenderer(num_scenes=2, tile_resolution=(32, 32))

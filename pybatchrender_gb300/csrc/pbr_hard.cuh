@@ -173,9 +173,9 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
   const int HW = W * H;
   const int words = A.tri_cap >> 5;
   const int B = A.bin_px;
-  // source triangles per round: every thread when a chunk holds THREADS records (a round that keeps more than
-  // a chunk is then placed in two halves of at most THREADS records each), else half a chunk
-  const int RT = A.tri_cap >= THREADS ? THREADS : (A.tri_cap >> 1);
+  // source triangles per round: one per thread, at most a chunk's records. A round keeps up to 2 * RT records
+  // (near-plane splits); one that keeps more than a chunk holds is placed in two halves of at most RT records.
+  const int RT = min(THREADS, A.tri_cap);
   const int IS = A.mvp_any ? 8 : 4;  // float4 per cached instance: model rows, colour [, view-projection x model rows]
 
   for (int it = 0;; ++it) {
@@ -767,9 +767,9 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
             place(c, incl, before, total);
           } else {
             // more kept records than a chunk holds (many near-plane splits): the round's two halves in draw order,
-            // each at most THREADS records (RT = THREADS only when tri_cap >= THREADS)
+            // RT / 2 source triangles each, so at most RT <= tri_cap records each
             for (int h = 0; h < 2; ++h) {
-              const int ch = ((tid < THREADS / 2) == (h == 0)) ? c : 0;
+              const int ch = ((tid < (RT >> 1)) == (h == 0)) ? c : 0;
               compact(ch, incl, before, total);
               place(ch, incl, before, total);
             }

@@ -191,11 +191,12 @@ def test_near_plane_clipping(cuda, oracle):
 
 
 def test_round_keeps_more_records_than_a_chunk(cuda, oracle):
-    """Tile kernel, 256 threads, 256-triangle chunks: one source triangle per
-    thread and round, and every triangle of the fan crosses the near plane, so
-    a round keeps 2 records per triangle (512 > 256).  The round is then placed
-    in two halves of 128 triangles, in draw order.  Against the oracle and
-    against 512-triangle chunks (where the round fits whole)."""
+    """Tile kernel: a round takes min(threads, chunk) source triangles, and
+    every triangle of the fan crosses the near plane, so a round keeps two
+    records per triangle, more than a chunk holds (256 threads with 256-triangle
+    chunks, 512 with 256, 128 with 64).  The round is then placed in two
+    halves, in draw order.  Against the oracle and against 256 threads with
+    512-triangle chunks, where every round fits whole."""
     from pybatchrender_gb300.renderer import meshes
     # 320 copies of one triangle (two vertices in front of the eye, one behind it), each turned about the
     # vertical axis through (0, 3, 0) and moved along the view axis, so that the copies cross one another
@@ -211,8 +212,8 @@ def test_round_keeps_more_records_than_a_chunk(cuda, oracle):
     nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
     fan = meshes.Mesh(pos.reshape(-1, 3), np.repeat(nrm, 3, 0), np.arange(960).reshape(-1, 3), name="fan")
     out = []
-    for cap in (256, 512):
-        r = pbr.PBRRenderer(num_scenes=2, tile_resolution=(64, 64), raster_kernel="tile", raster_threads=256,
+    for threads, cap in ((256, 512), (256, 256), (512, 256), (128, 64)):
+        r = pbr.PBRRenderer(num_scenes=2, tile_resolution=(64, 64), raster_kernel="tile", raster_threads=threads,
                             tri_cap=cap)
         node = r.add_node(fan, 1)
         node.set_colors(torch.tensor([[0.9, 0.5, 0.2, 1.0], [0.2, 0.7, 0.4, 1.0]]))
@@ -225,8 +226,9 @@ def test_round_keeps_more_records_than_a_chunk(cuda, oracle):
         # the fan faces the eye and covers most of the image, with many copies winning somewhere
         assert (ref["winner"] >= 0).mean() > 0.9 and len(np.unique(ref["winner"])) > 10, cmp
         out.append(gpu)
-    for key in ("pixels", "winner", "depth"):
-        assert np.array_equal(out[0][key], out[1][key])
+    for other in out[1:]:
+        for key in ("pixels", "winner", "depth"):
+            assert np.array_equal(out[0][key], other[key])
 
 
 def test_empty_and_degenerate_inputs(cuda, oracle):

@@ -20,10 +20,13 @@ constexpr int kInstWords = kMaxInstBatch / 32;
 
 enum : int { kModeHpr = 0, kModeRot = 1, kModeMat = 2 };
 
-// Device error flags (RasterArgs::status, OR-ed).
+// Device error flags (RasterArgs::status / SoftArgs::status, OR-ed; read and cleared by pbr_device_status).
+// The current kernels raise none of them: the planner rejects scenes whose winner ids would not fit in 31 bits
+// before any launch, and the tile kernel sizes its rounds so that a chunk always holds what it places.  The
+// values stay reserved for kernels that detect an error only on the device.
 enum : int {
-  kStatusIdOverflow = 1,   // winner id did not fit in 31 bits
-  kStatusCapacity = 2,     // a chunk could not hold one round of triangles
+  kStatusIdOverflow = 1,   // a winner id did not fit in 31 bits
+  kStatusCapacity = 2,     // a chunk could not hold what a round placed
 };
 
 constexpr int kClusterTris = 32;    // triangles per cluster (the last cluster of a mesh may hold fewer)

@@ -763,16 +763,18 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) hard_kernel(const __gr
           };
           int incl, before, total;
           compact(c, incl, before, total);
-          if (total <= A.tri_cap) {
-            place(c, incl, before, total);
-          } else {
-            // more kept records than a chunk holds (many near-plane splits): the round's two halves in draw order,
-            // RT / 2 source triangles each, so at most RT <= tri_cap records each
-            for (int h = 0; h < 2; ++h) {
-              const int ch = ((tid < (RT >> 1)) == (h == 0)) ? c : 0;
-              compact(ch, incl, before, total);
-              place(ch, incl, before, total);
+          // More kept records than a chunk holds (many near-plane splits): the round's two halves in draw order,
+          // RT / 2 source triangles each, so at most RT <= tri_cap records each.  One copy of place() serves both
+          // cases (it inlines the write pass; more copies cost instruction-cache misses in every launch).
+          const int pieces = total <= A.tri_cap ? 1 : 2;
+#pragma unroll 1
+          for (int h = 0; h < pieces; ++h) {
+            int n = c;
+            if (pieces == 2) {
+              n = ((tid < (RT >> 1)) == (h == 0)) ? c : 0;
+              compact(n, incl, before, total);
             }
+            place(n, incl, before, total);
           }
         }
         }  // sub-batches
